@@ -1,0 +1,322 @@
+"""Benchmark of the correction path (one JSON line on rank 0).
+
+Workload (default): plain single-field correction of a 512^3 fp64 Perlin fBm
+field (seed 1, 5 octaves, base frequency 1/64, persistence 0.5, lacunarity 2,
+normalised to [0,1]) decompressed through the ZFP-like stand-in at eps = 1e-4
+(the reference's per-rank weak-scaling block).  A step = one full correction
+(labelling, detection / edit sweeps to convergence) of that field.
+
+value   device-resident throughput, Gvox/s = N / (device time of one
+        pmsz_correct call), CUDA events on the launching stream, fhat refreshed
+        from a pristine device copy before each step (untimed).
+e2e     the same through the C ABI with host buffers: pinned host f and fhat
+        copied in, pmsz_correct, the corrected field copied back, all timed.
+roofline  the fused labelling + first detection pass (the dominant kernel):
+        algorithmic bytes N*(2*sizeof(T)+1) / its event-timed duration,
+        against the measured HBM copy bandwidth.
+cpu_baseline  the CPU oracle (a restatement of the reference loop, OpenMP on
+        all host cores) on a z-slab sample of the same field.
+
+--impl reference: the reference's path on the host cores -- the reference
+itself is CUDA-only with no CPU implementation, so this arm runs the CPU
+oracle restatement (kind "port") on the same slab sample.
+With N > 1 (torchrun) every rank corrects its own replica: no data-path
+collective; a barrier brackets the timed region and the max over ranks is taken.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gvox/s correction at 512³ fp64 vs ref 1-rank; batched vox/s; p50/p99 latency"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--shape", default="512,512,512", help="nx,ny,nz")
+    p.add_argument("--dtype", choices=["f32", "f64"], default="f64")
+    p.add_argument("--comp", choices=["sz3", "zfp"], default="zfp")
+    p.add_argument("--eb", type=float, default=1e-4)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--octaves", type=int, default=5)
+    p.add_argument("--base", type=float, default=1 / 64)
+    p.add_argument("--persistence", type=float, default=0.5)
+    p.add_argument("--cpu-slices", type=int, default=64, help="z-slices of the CPU sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=5)
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """dram read+write bytes per launch of `name` from a committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh).get(name)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_sample(f: np.ndarray, fh: np.ndarray, eb: float, slices: int):
+    """Time the CPU oracle on the first `slices` z-slices of the field."""
+    from oracle import oracle as O
+    fs = np.ascontiguousarray(f[:slices])
+    fhs = np.ascontiguousarray(fh[:slices])
+    t0 = time.perf_counter()
+    _, _, st, sweeps, _ = O.correct(fs, fhs, eb)
+    dt = time.perf_counter() - t0
+    return fs.size, dt, O.num_threads(), sweeps
+
+
+def gen_fields(args, torch, device, dtype):
+    from pmsz_anonymous_gb300 import api
+    nx, ny, nz = (int(v) for v in args.shape.split(","))
+    f = api.gen_perlin((nz, ny, nx), args.seed, args.octaves, args.base, args.persistence, 2.0,
+                       dtype=dtype, device=device)
+    fh = api.standin(f, args.eb, args.comp, args.seed)
+    torch.cuda.synchronize()
+    return f, fh
+
+
+def workload_config(args, extra=None):
+    nx, ny, nz = (int(v) for v in args.shape.split(","))
+    cfg = {"workload": f"plain single-field correction, {nx}x{ny}x{nz} {args.dtype} Perlin fBm "
+                       f"(seed {args.seed}, {args.octaves} octaves, base 1/{round(1 / args.base)}, "
+                       f"persistence {args.persistence}), {args.comp} stand-in, eps={args.eb:g}",
+           "shape": [nx, ny, nz], "dtype": args.dtype, "compressor": f"{args.comp} stand-in (compressor parity unpinned)",
+           "eb": args.eb, "q": 5, "l2": f"inputs {nx * ny * nz * (8 if args.dtype == 'f64' else 4) * 2 / 1e9:.2f} GB > 129 MB L2",
+           "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    from oracle import oracle as O
+    dtype = torch.float64 if args.dtype == "f64" else torch.float32
+    f, fh = gen_fields(args, torch, torch.device("cuda:0"), dtype)
+    fs, fhs = f[: args.cpu_slices].cpu().numpy(), fh[: args.cpu_slices].cpu().numpy()
+    del f, fh
+    times, n, thr = [], 0, 0
+    for i in range(args.warmup + args.steps):
+        n, dt, thr, sweeps = cpu_sample(fs, fhs, args.eb, args.cpu_slices)
+        if i >= args.warmup:
+            times.append(dt)
+    v = n / statistics.mean(times) / 1e9
+    sample = f"first {args.cpu_slices} z-slices ({n} voxels) of the field, CPU oracle restatement"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Gvox/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic", "config": workload_config(args, {"sample": sample}),
+        "cpu_baseline": {"value": v, "unit": "Gvox/s", "cores": thr, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's path is CUDA-only; its CPU arm is the oracle restatement of c_loops",
+    }), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from pmsz_anonymous_gb300 import _build, api
+    _build.build()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=device)
+    dtype = torch.float64 if args.dtype == "f64" else torch.float32
+    itemsize = 8 if args.dtype == "f64" else 4
+    f, fh0 = gen_fields(args, torch, device, dtype)
+    n = f.numel()
+    fh = torch.empty_like(fh0)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    first_ms, times, sweeps, launches = [], [], [], 0
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        fh.copy_(fh0)
+        api.correct(f, fh, args.eb)
+    barrier()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            fh.copy_(fh0)
+            start.record()
+            r = api.correct(f, fh, args.eb, timing=True)
+            stop.record()
+            stop.synchronize()
+            times.append(start.elapsed_time(stop))
+            first_ms.append(r.ms_first_pass)
+            sweeps.append(r.sweeps)
+            launches += r.launches
+            if r.status != 0:
+                raise RuntimeError(f"correction did not converge (status {r.status})")
+        barrier()
+        wall = time.perf_counter() - wall0
+    ms = statistics.mean(times)
+    if world > 1:
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3) / 1e9
+
+    # e2e through the C ABI from pinned host buffers
+    f_h = f.cpu().pin_memory()
+    fh_h = fh0.cpu().pin_memory()
+    out_h = torch.empty_like(fh_h).pin_memory()
+    fd, fhd = torch.empty_like(f), torch.empty_like(fh0)
+    e2e_times = []
+    for i in range(1 + args.e2e_steps):
+        barrier()
+        start.record()
+        fd.copy_(f_h, non_blocking=True)
+        fhd.copy_(fh_h, non_blocking=True)
+        api.correct(fd, fhd, args.eb)
+        out_h.copy_(fhd, non_blocking=True)
+        stop.record()
+        stop.synchronize()
+        if i:
+            e2e_times.append(start.elapsed_time(stop))
+    e2e_ms = statistics.mean(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    ok = api.verify(f, fhd, args.eb)
+
+    peak, peak_kind = measured_peaks()
+    bytes_first = n * (2 * itemsize + 1)
+    achieved = bytes_first / (statistics.mean(first_ms) * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+        "config": workload_config(args, {"sweeps": int(statistics.median(sweeps)),
+                                         "timing": "CUDA events around each pmsz_correct call; fhat refreshed "
+                                                   "from a device copy before each step (untimed)",
+                                         "wall_s_timed_region": wall}),
+        "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n * itemsize},
+        "roofline": {"bound": "hbm", "kernel": "k_detect_full<T,true> (labelling + first detection)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": bytes_first,
+                     "ms_per_launch": statistics.mean(first_ms),
+                     "traffic": profiled_traffic(f"first_pass_{args.dtype}")},
+        "gpu_launches": launches,
+        "verify": ok,
+    }
+    if rank == 0 and not args.no_cpu:
+        fs = f[: args.cpu_slices].cpu().numpy()
+        fhs = fh0[: args.cpu_slices].cpu().numpy()
+        cn, cdt, thr, _ = cpu_sample(fs, fhs, args.eb, args.cpu_slices)
+        out["cpu_baseline"] = {"value": cn / cdt / 1e9, "unit": "Gvox/s", "cores": thr, "kind": "port",
+                               "sample": f"first {args.cpu_slices} z-slices ({cn} voxels) of the same field, "
+                                         f"CPU oracle, {cdt:.2f} s"}
+    out["clocks"] = clk.summary()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

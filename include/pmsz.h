@@ -1,0 +1,182 @@
+/*
+ * pmsz.h -- C ABI of the GB300-native pMSz correction path.
+ *
+ * Plain pointers and sizes only.  Field pointers are DEVICE pointers owned by
+ * the caller; `stream` is a cudaStream_t passed as void* (NULL = the legacy
+ * default stream).  Every entry point returns a status code (PMSZ_OK = 0) and
+ * never aborts the process or the CUDA context; pmsz_last_error() describes
+ * the most recent failure on the calling thread.
+ *
+ * Fields are x-fastest, then y, then z: the raw layout the reference reads
+ * (read_subblock, pMSz.cu:274-313), without the reference's one-voxel padding
+ * -- the domain boundary is handled by in-domain tests, which is what the
+ * reference's INVALID_VAL halo encodes at an MPI grid of 1x1x1
+ * (pMSz.cu:346-381, 673-679, 709).
+ */
+#ifndef PMSZ_H
+#define PMSZ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMSZ_OK 0
+#define PMSZ_ERR_ARG 1            /* bad sizes / eb / q, NaN input, null pointer */
+#define PMSZ_ERR_OOM 2            /* device or host allocation failed */
+#define PMSZ_ERR_NOT_CONVERGED 3  /* max_sweeps reached, or a sweep changed nothing */
+#define PMSZ_ERR_CUDA 4           /* a CUDA runtime call failed */
+#define PMSZ_ERR_IO 5             /* file read / write failed (host helpers) */
+
+/* Sweep schedule flags. */
+#define PMSZ_FLAG_FULL_SWEEPS 1u  /* every detection sweep scans the whole field
+                                     (the reference's schedule) instead of only
+                                     voxels whose neighbourhood changed */
+#define PMSZ_FLAG_TIMING 2u       /* record CUDA events around every kernel on
+                                     `stream` and report per-kernel device time
+                                     in pmsz_result */
+
+typedef struct pmsz_opts {
+    int32_t q;           /* edit levels; the reference hard-codes q = 5 (pMSz.cu:2630) */
+    uint32_t flags;      /* PMSZ_FLAG_* */
+    int64_t max_sweeps;  /* cap on detection sweeps; the reference has none */
+} pmsz_opts;
+
+/* One record per detection sweep.  fmax / fmin / fdir are the reference's
+ * count_f_max / count_f_min / count_f_dir (pMSz.cu:174, 791-895), counted
+ * exactly. */
+typedef struct pmsz_sweep_record {
+    uint64_t fmax, fmin, fdir;
+    uint64_t requested;   /* distinct vertices edited in the sweep */
+    uint64_t changed;     /* ... whose value changed */
+    uint64_t progressed;  /* ... whose value or edit counter changed */
+    uint64_t active;      /* voxels the detection pass examined */
+    uint64_t bad;         /* NaN / 1e30-sentinel voxels seen (first sweep) */
+} pmsz_sweep_record;
+
+typedef struct pmsz_result {
+    int64_t sweeps;        /* detection sweeps run, including the final zero one */
+    int64_t iteration;     /* the value the reference prints as "iteration is:"
+                              (pMSz.cu:2073): sweeps + 1 at one rank */
+    uint64_t edits;        /* sum of `requested` over all sweeps */
+    pmsz_sweep_record *sweep_log;  /* optional host array, filled with min(sweeps,
+                                      sweep_log_cap) records */
+    int64_t sweep_log_cap;
+    /* With PMSZ_FLAG_TIMING (else 0): device milliseconds of the fused
+     * labelling + first detection pass, of all later detection passes, and of
+     * all edit passes; launches = kernels launched by the call. */
+    double ms_first_pass, ms_detect, ms_apply;
+    int64_t launches;
+} pmsz_result;
+
+/* Verification counts (replaces the reference's disabled check_consistency
+ * block, pMSz.cu:3038-3126, and count_false_cases, pMSz.cu:1852-1870). */
+typedef struct pmsz_verify_result {
+    uint64_t dir_mismatch;      /* voxels whose steepest asc or desc differs */
+    uint64_t ext_mismatch;      /* voxels whose max / min flag differs */
+    uint64_t as_mismatch;       /* voxels whose ascending-manifold label differs */
+    uint64_t ds_mismatch;       /* voxels whose descending-manifold label differs */
+    uint64_t bound_strict;      /* voxels with |f' - f| > eps evaluated in T */
+    uint64_t bound_beyond_clamp;/* voxels outside [fl(f - eps), fl(f + eps)]: the
+                                   reference's clamp value fl(f - eps) may sit up
+                                   to half an ulp beyond eps, so this count is
+                                   the one that must be zero */
+} pmsz_verify_result;
+
+/*
+ * pmsz_correct_{f32,f64}: the correction loop.  Replaces c_loops<T>
+ * (pMSz.cu:1872-2074) as called from main at pMSz.cu:2916, at an MPI grid of
+ * 1x1x1.  f is the original field, fhat its decompressed copy, corrected in
+ * place.  eb is the absolute error bound (argv[2], pMSz.cu:2628);
+ * delta = eb / q with the division in double (pMSz.cu:2814).  opts may be
+ * NULL (q = 5, no flags, max_sweeps = 10000); res may be NULL.
+ * Semantics are snapshot sweeps: every read of a sweep sees the field as it
+ * was when the sweep started, and each requested vertex is edited once per
+ * sweep with the arithmetic of applyDeltaBuffer_local (pMSz.cu:623-645).
+ * Library-owned scratch (direction codes, edit counters, bitmaps) is
+ * allocated stream-ordered on `stream` and released before return.
+ * Returns PMSZ_ERR_NOT_CONVERGED (fhat holds the last state) if max_sweeps is
+ * reached or a sweep requests edits that change nothing (every requested
+ * vertex already clamped), where the reference would loop forever.
+ */
+int pmsz_correct_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t nz,
+                     double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
+int pmsz_correct_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz,
+                     double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
+
+/*
+ * pmsz_codes_{f32,f64}: steepest-direction labelling of one field -- the
+ * neighbour scan and or_types encoding of iscriticle data_type=1
+ * (pMSz.cu:686-783).  codes[i] (device, n bytes): low nibble = stencil rank of
+ * the steepest ascent neighbour, high nibble = rank of the steepest descent
+ * neighbour (rank 7 = the voxel itself; see pmsz_rank_offset).
+ */
+int pmsz_codes_f32(const float *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, void *stream);
+int pmsz_codes_f64(const double *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, void *stream);
+
+/* (dx, dy, dz) of stencil rank r (0..14); returns PMSZ_ERR_ARG for other r. */
+int pmsz_rank_offset(int r, int *dx, int *dy, int *dz);
+
+/*
+ * pmsz_labels: ascending / descending manifold labels from direction codes by
+ * pointer jumping.  Replaces PathCompression (pMSz.cu:255-271; used in the
+ * loop by naive_MSz.cu:1914-1917, 2045-2047).  as_label / ds_label are device
+ * arrays of n uint32 flat indices of the maximum / minimum each voxel's
+ * steepest path reaches; either may be NULL.  Needs nx*ny*nz < 2^32.
+ */
+int pmsz_labels(const uint8_t *codes, size_t nx, size_t ny, size_t nz,
+                uint32_t *as_label, uint32_t *ds_label, void *stream);
+
+/* pmsz_verify_{f32,f64}: re-verification of a corrected field fp against f. */
+int pmsz_verify_f32(const float *f, const float *fp, size_t nx, size_t ny, size_t nz,
+                    double eb, pmsz_verify_result *out, void *stream);
+int pmsz_verify_f64(const double *f, const double *fp, size_t nx, size_t ny, size_t nz,
+                    double eb, pmsz_verify_result *out, void *stream);
+
+/*
+ * pmsz_extract_edits_{f32,f64}: edit output.  Replaces extract_edits_kernel +
+ * run_extract_edits + compact_edits_dense_to_sparse (pMSz.cu:2090-2226,
+ * 227-250).  Over the n voxels in x-fastest order, comparing the corrected
+ * field cur with the decompressed field prev:
+ *   cur == prev       -> deltas[i] = 0
+ *   cur == f - eps    -> deltas[i] = q; f - eps is appended to clamp[] unless 0
+ *   otherwise         -> deltas[i] = round((prev - cur) / delta)
+ * deltas (n bytes) and clamp (up to n values) are device arrays; *n_clamp and
+ * *edit_count (voxels with cur < prev, the reference's "Edit count") are
+ * written to host memory.  clamp keeps voxel order, like thrust::copy_if.
+ */
+int pmsz_extract_edits_f32(const float *prev, const float *cur, const float *f, size_t n,
+                           double eb, int q, uint8_t *deltas, float *clamp,
+                           uint64_t *n_clamp, uint64_t *edit_count, void *stream);
+int pmsz_extract_edits_f64(const double *prev, const double *cur, const double *f, size_t n,
+                           double eb, int q, uint8_t *deltas, double *clamp,
+                           uint64_t *n_clamp, uint64_t *edit_count, void *stream);
+
+/*
+ * Synthetic inputs (not part of the reference's path; its generator is
+ * generate_perlin.py).  pmsz_gen_perlin_*: normalised Perlin fBm, bit-identical
+ * to the numpy generator in pmsz_anonymous_gb300/fields.py.  perm512: host
+ * array of 512 int32; amps / freqs: host arrays of `octaves` doubles.
+ * pmsz_standin_*: decompressed stand-ins, kind 0 = "sz3" plateaus,
+ * kind 1 = "zfp" bounded noise (same bits as fields.py).
+ */
+int pmsz_gen_perlin_f32(float *out, size_t nx, size_t ny, size_t nz, const int32_t *perm512,
+                        const double *amps, const double *freqs, int octaves, void *stream);
+int pmsz_gen_perlin_f64(double *out, size_t nx, size_t ny, size_t nz, const int32_t *perm512,
+                        const double *amps, const double *freqs, int octaves, void *stream);
+int pmsz_standin_f32(const float *f, float *fhat, size_t n, double eb, int kind,
+                     uint64_t seed, void *stream);
+int pmsz_standin_f64(const double *f, double *fhat, size_t n, double eb, int kind,
+                     uint64_t seed, void *stream);
+
+/* Human-readable status, and the last error message of the calling thread. */
+const char *pmsz_strerror(int status);
+const char *pmsz_last_error(void);
+int pmsz_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMSZ_H */

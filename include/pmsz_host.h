@@ -1,0 +1,47 @@
+/*
+ * pmsz_host.h -- host-side helpers of the GB300-native pMSz path: the edit
+ * file encoder / decoder.  Host pointers only.  Buffers returned through
+ * `out` / `values` are allocated with malloc and released with pmsz_free.
+ */
+#ifndef PMSZ_HOST_H
+#define PMSZ_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "pmsz.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/*
+ * _deltas.bin payload.  Replaces compress_symbols_0_N (pMSz.cu:2359-2369)
+ * with pack_nbits / bits_for_max (pMSz.cu:2328-2356): each delta symbol in
+ * 0..q is packed LSB-first in bits_for_max(q) bits (3 bits for q = 5), then
+ * zstd level 5 (pMSz.cu:2480).
+ */
+int pmsz_encode_deltas(const uint8_t *deltas, size_t n, int q, uint8_t **out, size_t *out_len);
+
+/*
+ * _edits.bin payload.  Replaces compress_zstd<T> (pMSz.cu:2261-2277, called at
+ * pMSz.cu:2473): the clamp values as raw bytes (elem_size 4 or 8), zstd level
+ * 3; zero values give an empty payload (*out = NULL, *out_len = 0).
+ */
+int pmsz_encode_clamps(const void *values, size_t count, size_t elem_size, uint8_t **out, size_t *out_len);
+
+/* Inverses (the reference's decompress_symbols_0_N, pMSz.cu:2413-2426, and
+ * decompress_zstd_to_vector, pMSz.cu:2372-2391). */
+int pmsz_decode_deltas(const uint8_t *comp, size_t len, size_t n, int q, uint8_t *deltas);
+int pmsz_decode_clamps(const uint8_t *comp, size_t len, size_t elem_size, void **values, size_t *count);
+
+void pmsz_free(void *p);
+
+/* ZSTD_versionNumber() of the libzstd the library loaded (byte parity of the
+ * edit files holds only for equal zstd versions). */
+unsigned pmsz_zstd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMSZ_HOST_H */

@@ -1,0 +1,226 @@
+"""Python entry points over the C ABI, on torch CUDA tensors.
+
+Fields are contiguous tensors of shape (nz, ny, nx) (x fastest), float32 or
+float64, on a CUDA device.  Every call goes through libpmsz_gb300.so on the
+current torch stream; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import capi
+from . import fields as _fields
+
+SWEEP_KEYS = ("fmax", "fmin", "fdir", "requested", "changed", "progressed", "active", "bad")
+
+
+def _suffix(t: torch.Tensor) -> str:
+    if t.dtype == torch.float32:
+        return "f32"
+    if t.dtype == torch.float64:
+        return "f64"
+    raise TypeError(f"fields must be float32 or float64, got {t.dtype}")
+
+
+def _check_field(t: torch.Tensor, name: str):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dim() != 3 or not t.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous (nz, ny, nx) tensor")
+
+
+def _dims(t: torch.Tensor):
+    nz, ny, nx = t.shape
+    return int(nx), int(ny), int(nz)
+
+
+def _stream(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+@dataclass
+class CorrectResult:
+    status: int
+    sweeps: int
+    iteration: int
+    edits: int
+    log: np.ndarray = field(repr=False)  # (sweeps, 8) uint64, columns SWEEP_KEYS
+    ms_first_pass: float = 0.0
+    ms_detect: float = 0.0
+    ms_apply: float = 0.0
+    launches: int = 0
+
+    @property
+    def converged(self) -> bool:
+        return self.status == capi.PMSZ_OK
+
+
+def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
+            full_sweeps: bool = False, timing: bool = False, stream=None) -> CorrectResult:
+    """Correct fhat in place so that its extrema and both segmentations match f
+    (c_loops, pMSz.cu:1872-2074).  Raises PmszError except for
+    PMSZ_ERR_NOT_CONVERGED, which is reported in the result."""
+    _check_field(f, "f")
+    _check_field(fhat, "fhat")
+    if f.shape != fhat.shape or f.dtype != fhat.dtype or f.device != fhat.device:
+        raise ValueError("f and fhat must share shape, dtype and device")
+    L = capi.load()
+    flags = (capi.PMSZ_FLAG_FULL_SWEEPS if full_sweeps else 0) | (capi.PMSZ_FLAG_TIMING if timing else 0)
+    opts = capi.Opts(int(q), flags, int(max_sweeps))
+    log = (capi.SweepRecord * int(max_sweeps))()
+    res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
+    nx, ny, nz = _dims(f)
+    with torch.cuda.device(f.device):
+        st = getattr(L, f"pmsz_correct_{_suffix(f)}")(
+            f.data_ptr(), fhat.data_ptr(), nx, ny, nz, float(eb), ctypes.byref(opts), ctypes.byref(res),
+            _stream(stream))
+    capi.check(st, allow=(capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED))
+    n = int(res.sweeps)
+    rows = np.array([[getattr(log[i], k) for k in SWEEP_KEYS] for i in range(n)],
+                    dtype=np.uint64).reshape(n, len(SWEEP_KEYS))
+    return CorrectResult(st, n, int(res.iteration), int(res.edits), rows, float(res.ms_first_pass),
+                         float(res.ms_detect), float(res.ms_apply), int(res.launches))
+
+
+def codes(v: torch.Tensor, stream=None) -> torch.Tensor:
+    """Steepest-direction code byte of every voxel (iscriticle data_type=1)."""
+    _check_field(v, "v")
+    out = torch.empty(v.shape, dtype=torch.uint8, device=v.device)
+    nx, ny, nz = _dims(v)
+    with torch.cuda.device(v.device):
+        capi.check(getattr(capi.load(), f"pmsz_codes_{_suffix(v)}")(v.data_ptr(), nx, ny, nz, out.data_ptr(),
+                                                                    _stream(stream)))
+    return out
+
+
+def rank_offsets() -> np.ndarray:
+    """(15, 3) int array of the (dx, dy, dz) of each stencil rank."""
+    L = capi.load()
+    out = np.zeros((15, 3), np.int64)
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    for r in range(15):
+        capi.check(L.pmsz_rank_offset(r, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        out[r] = (a.value, b.value, c.value)
+    return out
+
+
+def labels(code: torch.Tensor, stream=None):
+    """(AS labels, DS labels) as int64 flat indices, by pointer jumping."""
+    if code.dtype != torch.uint8 or code.dim() != 3 or not code.is_cuda:
+        raise TypeError("codes must be a (nz, ny, nx) uint8 CUDA tensor")
+    nz, ny, nx = code.shape
+    a = torch.empty(code.shape, dtype=torch.int32, device=code.device)
+    d = torch.empty(code.shape, dtype=torch.int32, device=code.device)
+    with torch.cuda.device(code.device):
+        capi.check(capi.load().pmsz_labels(code.data_ptr(), nx, ny, nz, a.data_ptr(), d.data_ptr(), _stream(stream)))
+    mask = (1 << 32) - 1
+    return a.to(torch.int64) & mask, d.to(torch.int64) & mask
+
+
+def verify(f: torch.Tensor, fp: torch.Tensor, eb: float, stream=None) -> dict:
+    _check_field(f, "f")
+    _check_field(fp, "fp")
+    out = capi.VerifyResult()
+    nx, ny, nz = _dims(f)
+    with torch.cuda.device(f.device):
+        capi.check(getattr(capi.load(), f"pmsz_verify_{_suffix(f)}")(
+            f.data_ptr(), fp.data_ptr(), nx, ny, nz, float(eb), ctypes.byref(out), _stream(stream)))
+    return {k: int(getattr(out, k)) for k, _ in capi.VerifyResult._fields_}
+
+
+def extract_edits(prev: torch.Tensor, cur: torch.Tensor, f: torch.Tensor, eb: float, q: int = 5, stream=None):
+    """(deltas uint8 tensor, clamp-value tensor, edit_count)."""
+    n = prev.numel()
+    deltas = torch.empty(n, dtype=torch.uint8, device=prev.device)
+    clamp = torch.empty(n, dtype=prev.dtype, device=prev.device)
+    nc, ec = ctypes.c_uint64(), ctypes.c_uint64()
+    with torch.cuda.device(prev.device):
+        capi.check(getattr(capi.load(), f"pmsz_extract_edits_{_suffix(prev)}")(
+            prev.data_ptr(), cur.data_ptr(), f.data_ptr(), n, float(eb), int(q), deltas.data_ptr(),
+            clamp.data_ptr(), ctypes.byref(nc), ctypes.byref(ec), _stream(stream)))
+    return deltas, clamp[: nc.value], int(ec.value)
+
+
+def gen_perlin(shape, seed: int, octaves: int, base_freq: float, persistence: float = 0.5,
+               lacunarity: float = 2.0, dtype=torch.float32, device="cuda", stream=None) -> torch.Tensor:
+    """Normalised Perlin fBm on the device (same bits as fields.perlin_field)."""
+    nz, ny, nx = shape
+    out = torch.empty(shape, dtype=dtype, device=device)
+    perm = np.ascontiguousarray(_fields.permutation(seed), dtype=np.int32)
+    amps, freqs = _fields.octave_table(octaves, base_freq, persistence, lacunarity)
+    with torch.cuda.device(out.device):
+        capi.check(getattr(capi.load(), f"pmsz_gen_perlin_{_suffix(out)}")(
+            out.data_ptr(), nx, ny, nz, perm.ctypes.data, amps.ctypes.data, freqs.ctypes.data, int(octaves),
+            _stream(stream)))
+    return out
+
+
+def standin(f: torch.Tensor, eb: float, compressor: str, seed: int = 0, stream=None) -> torch.Tensor:
+    """Decompressed stand-in of f ("sz3" plateaus or "zfp" noise), same bits as fields.standin."""
+    kind = {"sz3": 0, "zfp": 1}.get(compressor)
+    if kind is None:
+        raise ValueError(f"unknown compressor {compressor!r} (expected 'sz3' or 'zfp')")
+    out = torch.empty_like(f)
+    with torch.cuda.device(f.device):
+        capi.check(getattr(capi.load(), f"pmsz_standin_{_suffix(f)}")(
+            f.data_ptr(), out.data_ptr(), f.numel(), float(eb), kind, int(seed), _stream(stream)))
+    return out
+
+
+# ---- host encoders (no GPU needed) -------------------------------------------------------------
+
+def _take(L, ptr: ctypes.c_void_p, n: int) -> bytes:
+    if not ptr.value or n == 0:
+        return b""
+    data = ctypes.string_at(ptr.value, n)
+    L.pmsz_free(ptr)
+    return data
+
+
+def encode_deltas(deltas: np.ndarray, q: int = 5) -> bytes:
+    """_deltas.bin payload: bit-packed delta symbols, zstd level 5."""
+    L = capi.load()
+    d = np.ascontiguousarray(deltas, dtype=np.uint8).ravel()
+    out, n = ctypes.c_void_p(), ctypes.c_size_t()
+    capi.check(L.pmsz_encode_deltas(d.ctypes.data, d.size, int(q), ctypes.byref(out), ctypes.byref(n)))
+    return _take(L, out, n.value)
+
+
+def encode_clamps(values: np.ndarray) -> bytes:
+    """_edits.bin payload: raw clamp values, zstd level 3 (empty for none)."""
+    L = capi.load()
+    v = np.ascontiguousarray(values)
+    if v.dtype not in (np.float32, np.float64):
+        raise TypeError("clamp values must be float32 or float64")
+    out, n = ctypes.c_void_p(), ctypes.c_size_t()
+    capi.check(L.pmsz_encode_clamps(v.ctypes.data if v.size else None, v.size, v.itemsize,
+                                    ctypes.byref(out), ctypes.byref(n)))
+    return _take(L, out, n.value)
+
+
+def decode_deltas(blob: bytes, n: int, q: int = 5) -> np.ndarray:
+    L = capi.load()
+    out = np.empty(n, np.uint8)
+    buf = np.frombuffer(blob, np.uint8)
+    capi.check(L.pmsz_decode_deltas(buf.ctypes.data if buf.size else None, buf.size, n, int(q), out.ctypes.data))
+    return out
+
+
+def decode_clamps(blob: bytes, dtype) -> np.ndarray:
+    L = capi.load()
+    dt = np.dtype(dtype)
+    buf = np.frombuffer(blob, np.uint8)
+    out, cnt = ctypes.c_void_p(), ctypes.c_size_t()
+    capi.check(L.pmsz_decode_clamps(buf.ctypes.data if buf.size else None, buf.size, dt.itemsize,
+                                    ctypes.byref(out), ctypes.byref(cnt)))
+    raw = _take(L, out, cnt.value * dt.itemsize)
+    return np.frombuffer(raw, dt).copy()
+
+
+def zstd_version() -> int:
+    return int(capi.load().pmsz_zstd_version())

@@ -1,0 +1,435 @@
+// correct.cu -- labelling, detection and edit kernels and the correction loop.
+//
+// Replaces iscriticle (pMSz.cu:649-899), applyDeltaBuffer_local
+// (pMSz.cu:623-645), init_edits / init_counter (pMSz.cu:902-906, 1745-1749) and
+// the host loop c_loops (pMSz.cu:1872-2074) at an MPI grid of 1x1x1.
+//
+// Sweep k (snapshot semantics):
+//   detect   every voxel u of the active set A_k reads fhat on its closed
+//            stencil N[u] and the original direction code of u, applies the
+//            reference rules, ORs the vertices it wants lowered into the
+//            request bitmap R, and sets u in M_k (the next active bitmap) if
+//            it mismatched.
+//   apply    every vertex in R is edited once (applyDeltaBuffer_local); R is
+//            cleared; the closed stencil of every vertex whose value changed
+//            is ORed into the next active bitmap.
+// A voxel whose stencil did not change keeps its previous outcome, so
+// A_{k+1} = M_k U N[C_k] (C_k = changed vertices) yields exactly the requests
+// and counters of a full sweep over all voxels.  Sweep 1 is a full pass fused
+// with the original labelling: it reads f and fhat once and writes the codes.
+// PMSZ_FLAG_FULL_SWEEPS replaces the active set by the whole field.
+#include "common.cuh"
+#include "../../include/pmsz.h"
+#include "internal.h"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace pmsz {
+
+// ---------------------------------------------------------------------------
+// Stencil loads.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void load_keys(const T *__restrict__ v, size_t i, const Geom &g,
+                                          uint32_t valid, typename KeyOf<T>::type (&k)[15]) {
+    const ptrdiff_t sx = 1, sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
+#pragma unroll
+    for (int r = 0; r < 15; ++r) {
+        const ptrdiff_t off = rank_dx(r) * sx + rank_dy(r) * sy + rank_dz(r) * sz;
+        k[r] = ((valid >> r) & 1u) ? okey(__ldg(v + (static_cast<ptrdiff_t>(i) + off)))
+                                   : typename KeyOf<T>::type(0);
+    }
+}
+
+__device__ __forceinline__ void request_targets(uint32_t *__restrict__ req, const Geom &g, int x, int y,
+                                                int z, uint32_t tm) {
+    while (tm) {
+        const int r = __ffs(tm) - 1;
+        tm &= tm - 1;
+        const int tx = x + rank_dx(r), ty = y + rank_dy(r), tz = z + rank_dz(r);
+        atomicOr(req + word_of(g, tx, ty, tz), 1u << (tx & 31));
+    }
+}
+
+__device__ __forceinline__ void flush_counts(SweepSlot *slot, uint32_t cmax, uint32_t cmin,
+                                             uint32_t cdir, uint32_t active, uint32_t bad) {
+    cmax = warp_sum_u32(cmax);
+    cmin = warp_sum_u32(cmin);
+    cdir = warp_sum_u32(cdir);
+    active = warp_sum_u32(active);
+    bad = warp_sum_u32(bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (cmax) atomicAdd(&slot->fmax, (unsigned long long)cmax);
+        if (cmin) atomicAdd(&slot->fmin, (unsigned long long)cmin);
+        if (cdir) atomicAdd(&slot->fdir, (unsigned long long)cdir);
+        if (active) atomicAdd(&slot->active, (unsigned long long)active);
+        if (bad) atomicAdd(&slot->bad, (unsigned long long)bad);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Full detection pass over a 3-D grid: block (32, 8), one warp per 32-voxel
+// x-segment, which is exactly one bitmap word.  FIRST: also label the
+// original field f and store the code byte (iscriticle data_type=1 fused with
+// the first data_type=0 pass).
+// ---------------------------------------------------------------------------
+template <typename T, bool FIRST>
+__global__ void __launch_bounds__(256) k_detect_full(const T *__restrict__ f, const T *__restrict__ fh,
+                                                     uint8_t *__restrict__ codes, uint32_t *__restrict__ req,
+                                                     uint32_t *__restrict__ act_next, SweepSlot *slot, Geom g) {
+    using K = typename KeyOf<T>::type;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const bool in = x < g.nx && y < g.ny;
+    uint32_t cmax = 0, cmin = 0, cdir = 0, bad = 0;
+    uint32_t tm = 0;
+    if (in) {
+        const size_t i = flat(g, x, y, z);
+        const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        int oasc, odesc;
+        K k[15];
+        if (FIRST) {
+            load_keys(f, i, g, valid, k);
+            arg_ext(k, valid, oasc, odesc);
+            codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
+            bad = bad_value(f[i]) || bad_value(fh[i]);
+        } else {
+            const uint8_t c = codes[i];
+            oasc = c & 15;
+            odesc = c >> 4;
+        }
+        int asc, desc;
+        load_keys(fh, i, g, valid, k);
+        arg_ext(k, valid, asc, desc);
+        tm = detect_rules(asc, desc, oasc, odesc, cmax, cmin, cdir);
+        if (tm) request_targets(req, g, x, y, z, tm);
+    }
+    const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
+    if (threadIdx.x == 0 && y < g.ny && mism) act_next[word_of(g, blockIdx.x * 32, y, z)] = mism;
+    flush_counts(slot, cmax, cmin, cdir, in ? 1u : 0u, bad);
+}
+
+// ---------------------------------------------------------------------------
+// Sparse detection over the active bitmap (grid-stride over words).  The
+// word's bits are consumed and cleared; mismatching voxels go to act_next
+// (only this thread touches that word of act_next in this kernel).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_detect_sparse(const T *__restrict__ fh, const uint8_t *__restrict__ codes,
+                                                       uint32_t *__restrict__ act_cur, uint32_t *__restrict__ act_next,
+                                                       uint32_t *__restrict__ req, SweepSlot *slot, Geom g) {
+    using K = typename KeyOf<T>::type;
+    uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t w = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < g.nwords; w += stride) {
+        uint32_t bits = act_cur[w];
+        if (!bits) continue;
+        act_cur[w] = 0;
+        const size_t row = w / g.wpr;
+        const int wx = static_cast<int>(w - row * g.wpr);
+        const int y = static_cast<int>(row % g.ny);
+        const int z = static_cast<int>(row / g.ny);
+        uint32_t mism = 0;
+        active += __popc(bits);
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int x = wx * 32 + b;
+            const size_t i = flat(g, x, y, z);
+            const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+            K k[15];
+            load_keys(fh, i, g, valid, k);
+            int asc, desc;
+            arg_ext(k, valid, asc, desc);
+            const uint8_t c = codes[i];
+            const uint32_t tm = detect_rules(asc, desc, c & 15, c >> 4, cmax, cmin, cdir);
+            if (tm) {
+                request_targets(req, g, x, y, z, tm);
+                mism |= 1u << b;
+            }
+        }
+        if (mism) act_next[w] = mism;
+    }
+    flush_counts(slot, cmax, cmin, cdir, active, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Apply: applyDeltaBuffer_local (pMSz.cu:623-645) on every requested vertex,
+// in T:  if |f - (fhat - delta)| <= eps && cnt < q-1 { fhat -= delta; cnt++ }
+//        else { cnt = q; fhat = f - eps }
+// then mark the closed stencil of every vertex whose value changed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void or_word(uint32_t *act, const Geom &g, int wx, int y, int z, uint32_t m) {
+    if (!m || wx < 0 || wx >= g.wpr || y < 0 || y >= g.ny || z < 0 || z >= g.nz) return;
+    m &= row_tail_mask(g, wx);
+    if (m) atomicOr(act + static_cast<size_t>(wx) + static_cast<size_t>(g.wpr) * (static_cast<size_t>(y) + static_cast<size_t>(g.ny) * z), m);
+}
+
+// Closed-stencil dilation of the changed bits c of word (wx, y, z).  Rows
+// (dy,dz) = (0,0) take x-1..x+1; (1,0),(0,1),(1,1) take x-1,x; (-1,0),(0,-1),
+// (-1,-1) take x,x+1 -- the 15 offsets of the stencil.
+__device__ __forceinline__ void mark_stencil(uint32_t *act, const Geom &g, int wx, int y, int z, uint32_t c) {
+    const uint32_t lo = (c & 1u) << 31;  // x-1 of bit 0 lands in word wx-1
+    const uint32_t hi = c >> 31;         // x+1 of bit 31 lands in word wx+1
+    or_word(act, g, wx, y, z, c | (c << 1) | (c >> 1));
+    or_word(act, g, wx - 1, y, z, lo);
+    or_word(act, g, wx + 1, y, z, hi);
+    const uint32_t m = c | (c >> 1), p = c | (c << 1);
+    or_word(act, g, wx, y + 1, z, m);     or_word(act, g, wx - 1, y + 1, z, lo);
+    or_word(act, g, wx, y, z + 1, m);     or_word(act, g, wx - 1, y, z + 1, lo);
+    or_word(act, g, wx, y + 1, z + 1, m); or_word(act, g, wx - 1, y + 1, z + 1, lo);
+    or_word(act, g, wx, y - 1, z, p);     or_word(act, g, wx + 1, y - 1, z, hi);
+    or_word(act, g, wx, y, z - 1, p);     or_word(act, g, wx + 1, y, z - 1, hi);
+    or_word(act, g, wx, y - 1, z - 1, p); or_word(act, g, wx + 1, y - 1, z - 1, hi);
+}
+
+__device__ __forceinline__ uint64_t bits_of(double v) { return static_cast<uint64_t>(__double_as_longlong(v)); }
+__device__ __forceinline__ uint64_t bits_of(float v) { return __float_as_uint(v); }
+
+template <typename T>
+__device__ __forceinline__ uint32_t apply_one(const T *__restrict__ f, T *__restrict__ fh, uint8_t *__restrict__ cnt,
+                                              size_t v, T eps, T delta, int q, bool &progressed) {
+    const T old = fh[v];
+    const uint8_t oc = cnt[v];
+    const T lowered = old - delta;
+    const T fv = f[v];
+    T nv;
+    uint8_t nc;
+    if (fabs(fv - lowered) <= eps && static_cast<int>(oc) < q - 1) {
+        nv = lowered;
+        nc = static_cast<uint8_t>(oc + 1);
+    } else {
+        nc = static_cast<uint8_t>(q);
+        nv = fv - eps;
+    }
+    fh[v] = nv;
+    cnt[v] = nc;
+    const bool vchg = bits_of(old) != bits_of(nv);
+    progressed = vchg || nc != oc;
+    return vchg ? 1u : 0u;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_apply(const T *__restrict__ f, T *__restrict__ fh, uint8_t *__restrict__ cnt,
+                                               uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                               SweepSlot *slot, Geom g, T eps, T delta, int q) {
+    uint32_t nreq = 0, nchg = 0, nprog = 0;
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t w = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < g.nwords; w += stride) {
+        uint32_t bits = req[w];
+        if (!bits) continue;
+        req[w] = 0;
+        const size_t row = w / g.wpr;
+        const int wx = static_cast<int>(w - row * g.wpr);
+        const int y = static_cast<int>(row % g.ny);
+        const int z = static_cast<int>(row / g.ny);
+        nreq += __popc(bits);
+        uint32_t changed = 0;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            bool prog;
+            const uint32_t c = apply_one(f, fh, cnt, flat(g, wx * 32 + b, y, z), eps, delta, q, prog);
+            changed |= c << b;
+            nprog += prog ? 1u : 0u;
+        }
+        nchg += __popc(changed);
+        if (changed) mark_stencil(act_next, g, wx, y, z, changed);
+    }
+    nreq = warp_sum_u32(nreq);
+    nchg = warp_sum_u32(nchg);
+    nprog = warp_sum_u32(nprog);
+    if ((threadIdx.x & 31) == 0) {
+        if (nreq) atomicAdd(&slot->requested, (unsigned long long)nreq);
+        if (nchg) atomicAdd(&slot->changed, (unsigned long long)nchg);
+        if (nprog) atomicAdd(&slot->progressed, (unsigned long long)nprog);
+    }
+}
+
+// Codes only (pmsz_codes): the labelling half of the first pass.
+template <typename T>
+__global__ void __launch_bounds__(256) k_codes(const T *__restrict__ v, uint8_t *__restrict__ codes, Geom g) {
+    using K = typename KeyOf<T>::type;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= g.nx || y >= g.ny) return;
+    const size_t i = flat(g, x, y, z);
+    const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+    K k[15];
+    load_keys(v, i, g, valid, k);
+    int a, d;
+    arg_ext(k, valid, a, d);
+    codes[i] = static_cast<uint8_t>(a | (d << 4));
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+static inline dim3 grid3(const Geom &g) {
+    return dim3(static_cast<unsigned>(g.wpr), static_cast<unsigned>((g.ny + 7) / 8), static_cast<unsigned>(g.nz));
+}
+
+static inline unsigned stride_grid(size_t items) {
+    const size_t want = (items + 255) / 256;
+    return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(want, 152 * 16)));
+}
+
+int check_geom(size_t nx, size_t ny, size_t nz) {
+    if (nx == 0 || ny == 0 || nz == 0) return set_error(PMSZ_ERR_ARG, "field dimensions must be positive");
+    if (nx > (1u << 30) || ny > 65535 * 8 || nz > 65535)
+        return set_error(PMSZ_ERR_ARG, "field dimensions exceed the supported range (nz <= 65535)");
+    return PMSZ_OK;
+}
+
+template <typename T>
+int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
+                 pmsz_result *res, cudaStream_t s) {
+    if (!f || !fh) return set_error(PMSZ_ERR_ARG, "null field pointer");
+    int rc = check_geom(nx, ny, nz);
+    if (rc) return rc;
+    const int q = opts ? opts->q : 5;
+    const uint32_t flags = opts ? opts->flags : 0u;
+    const int64_t max_sweeps = opts && opts->max_sweeps > 0 ? opts->max_sweeps : 10000;
+    if (!(eb > 0.0) || !(eb < 1e300)) return set_error(PMSZ_ERR_ARG, "error bound must be positive and finite");
+    if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
+    const Geom g = make_geom(nx, ny, nz);
+    const T eps = static_cast<T>(eb);
+    const T delta = static_cast<T>(eb / static_cast<double>(q));  // pMSz.cu:2814
+
+    // Scratch: codes (n), counters (n), request + two active bitmaps, sweep slots.
+    Workspace ws(s);
+    const size_t o_codes = ws.reserve<uint8_t>(g.n);
+    const size_t o_cnt = ws.reserve<uint8_t>(g.n);
+    const size_t o_req = ws.reserve<uint32_t>(g.nwords);
+    const size_t o_a0 = ws.reserve<uint32_t>(g.nwords);
+    const size_t o_a1 = ws.reserve<uint32_t>(g.nwords);
+    const size_t o_slots = ws.reserve<SweepSlot>(static_cast<size_t>(max_sweeps));
+    if ((rc = ws.commit())) return rc;
+    uint8_t *codes = ws.at<uint8_t>(o_codes);
+    uint8_t *cnt = ws.at<uint8_t>(o_cnt);
+    uint32_t *req = ws.at<uint32_t>(o_req);
+    uint32_t *act[2] = {ws.at<uint32_t>(o_a0), ws.at<uint32_t>(o_a1)};
+    SweepSlot *slots = ws.at<SweepSlot>(o_slots);
+
+    PMSZ_CUDA(cudaMemsetAsync(cnt, 0, g.n, s));  // init_counter, pMSz.cu:1745-1749
+    PMSZ_CUDA(cudaMemsetAsync(req, 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
+
+    SweepSlot *hslot = static_cast<SweepSlot *>(host_pinned(sizeof(SweepSlot)));
+    if (!hslot) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+    const bool timing = (flags & PMSZ_FLAG_TIMING) != 0;
+    EventTimer et;
+    if (timing && (rc = et.init())) return rc;
+    double ms_first = 0, ms_detect = 0, ms_apply = 0;
+    int64_t launches = 0;
+    const dim3 blk3(32, 8, 1);
+    int cur = 0;  // act[cur] = active set of the coming sweep; act[cur^1] receives the next one
+    int64_t sweeps = 0;
+    uint64_t edits = 0;
+    int status = PMSZ_ERR_NOT_CONVERGED;
+    std::vector<SweepSlot> log;
+    while (sweeps < max_sweeps) {
+        SweepSlot *slot = slots + sweeps;
+        uint32_t *a_next = act[cur ^ 1];
+        if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+        if (sweeps == 0) {
+            k_detect_full<T, true><<<grid3(g), blk3, 0, s>>>(f, fh, codes, req, a_next, slot, g);
+        } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
+            k_detect_full<T, false><<<grid3(g), blk3, 0, s>>>(nullptr, fh, codes, req, a_next, slot, g);
+        } else {
+            k_detect_sparse<T><<<stride_grid(g.nwords), 256, 0, s>>>(fh, codes, act[cur], a_next, req, slot, g);
+        }
+        if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
+        k_apply<T><<<stride_grid(g.nwords), 256, 0, s>>>(f, fh, cnt, req, a_next, slot, g, eps, delta, q);
+        if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[2], s));
+        launches += 2;
+        PMSZ_CUDA(cudaGetLastError());
+        PMSZ_CUDA(cudaMemcpyAsync(hslot, slot, sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        if (timing) {
+            float a = 0, b = 0;
+            PMSZ_CUDA(cudaEventElapsedTime(&a, et.ev[0], et.ev[1]));
+            PMSZ_CUDA(cudaEventElapsedTime(&b, et.ev[1], et.ev[2]));
+            (sweeps == 0 ? ms_first : ms_detect) += a;
+            ms_apply += b;
+        }
+        ++sweeps;
+        const SweepSlot h = *hslot;
+        log.push_back(h);
+        edits += h.requested;
+        if (sweeps == 1 && h.bad) {
+            status = set_error(PMSZ_ERR_ARG, "input contains NaN or the value 1e30 (the reference's halo sentinel)");
+            break;
+        }
+        if (h.fmax == 0 && h.fmin == 0 && h.fdir == 0) { status = PMSZ_OK; break; }
+        if (h.progressed == 0) {
+            set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
+            break;
+        }
+        cur ^= 1;
+    }
+    if (status == PMSZ_ERR_NOT_CONVERGED && sweeps >= max_sweeps)
+        set_error(PMSZ_ERR_NOT_CONVERGED, "max_sweeps reached before convergence");
+    if (res) {
+        res->sweeps = sweeps;
+        res->iteration = sweeps + 1;
+        res->edits = edits;
+        res->ms_first_pass = ms_first;
+        res->ms_detect = ms_detect;
+        res->ms_apply = ms_apply;
+        res->launches = launches;
+        if (res->sweep_log && res->sweep_log_cap > 0) {
+            const size_t m = std::min<size_t>(log.size(), static_cast<size_t>(res->sweep_log_cap));
+            static_assert(sizeof(SweepSlot) == sizeof(pmsz_sweep_record), "record layout");
+            std::memcpy(res->sweep_log, log.data(), m * sizeof(SweepSlot));
+        }
+    }
+    rc = ws.release();
+    return status != PMSZ_OK ? status : rc;
+}
+
+template <typename T>
+int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cudaStream_t s) {
+    if (!v || !codes) return set_error(PMSZ_ERR_ARG, "null pointer");
+    int rc = check_geom(nx, ny, nz);
+    if (rc) return rc;
+    const Geom g = make_geom(nx, ny, nz);
+    k_codes<T><<<grid3(g), dim3(32, 8, 1), 0, s>>>(v, codes, g);
+    PMSZ_CUDA(cudaGetLastError());
+    return PMSZ_OK;
+}
+
+template int codes_impl<float>(const float *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
+template int codes_impl<double>(const double *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
+
+}  // namespace pmsz
+
+using namespace pmsz;
+
+extern "C" int pmsz_correct_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                                const pmsz_opts *opts, pmsz_result *res, void *stream) {
+    return guarded([&] { return correct_impl<float>(f, fhat, nx, ny, nz, eb, opts, res, as_stream(stream)); });
+}
+extern "C" int pmsz_correct_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                                const pmsz_opts *opts, pmsz_result *res, void *stream) {
+    return guarded([&] { return correct_impl<double>(f, fhat, nx, ny, nz, eb, opts, res, as_stream(stream)); });
+}
+extern "C" int pmsz_codes_f32(const float *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, void *stream) {
+    return guarded([&] { return codes_impl<float>(v, nx, ny, nz, codes, as_stream(stream)); });
+}
+extern "C" int pmsz_codes_f64(const double *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, void *stream) {
+    return guarded([&] { return codes_impl<double>(v, nx, ny, nz, codes, as_stream(stream)); });
+}
+extern "C" int pmsz_rank_offset(int r, int *dx, int *dy, int *dz) {
+    if (r < 0 || r > 14 || !dx || !dy || !dz) return PMSZ_ERR_ARG;
+    *dx = rank_dx(r);
+    *dy = rank_dy(r);
+    *dz = rank_dz(r);
+    return PMSZ_OK;
+}

@@ -1,0 +1,91 @@
+// internal.h -- host-side plumbing shared by the C-ABI translation units:
+// thread-local error messages, exception fencing, stream-ordered scratch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/pmsz.h"
+
+namespace pmsz {
+
+// Records `msg` as the calling thread's last error and returns `status`.
+int set_error(int status, const std::string &msg);
+
+#define PMSZ_CUDA(expr)                                                                       \
+    do {                                                                                      \
+        cudaError_t e_ = (expr);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return ::pmsz::set_error(PMSZ_ERR_CUDA, std::string(#expr " failed: ") +         \
+                                                        cudaGetErrorString(e_));              \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// No exception crosses the C ABI.
+template <class F>
+int guarded(F &&fn) noexcept {
+    try {
+        return fn();
+    } catch (const std::bad_alloc &) {
+        return set_error(PMSZ_ERR_OOM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return set_error(PMSZ_ERR_ARG, e.what());
+    } catch (...) {
+        return set_error(PMSZ_ERR_ARG, "unknown exception");
+    }
+}
+
+// Keeps the device's default memory pool from returning freed blocks to the
+// driver, so repeated calls reuse scratch without new allocations.
+void retain_pool_once();
+
+// Stream-ordered scratch: reserve() sizes, commit() makes one cudaMallocAsync
+// on the call's stream, at<T>() hands out 256-byte aligned sub-ranges, the
+// destructor frees stream-ordered.
+class Workspace {
+public:
+    explicit Workspace(cudaStream_t s) : s_(s) {}
+    ~Workspace() { release(); }
+    Workspace(const Workspace &) = delete;
+    Workspace &operator=(const Workspace &) = delete;
+
+    template <class T>
+    size_t reserve(size_t count) {
+        const size_t off = total_;
+        total_ += (count * sizeof(T) + 255) & ~static_cast<size_t>(255);
+        return off;
+    }
+    int commit();
+    template <class T>
+    T *at(size_t off) const { return reinterpret_cast<T *>(base_ + off); }
+    int release();
+
+private:
+    cudaStream_t s_;
+    size_t total_ = 0;
+    char *base_ = nullptr;
+};
+
+// A few CUDA events for per-kernel timing, destroyed with the object.
+struct EventTimer {
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int init() {
+        for (auto &e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return set_error(PMSZ_ERR_CUDA, "cudaEventCreate failed");
+        return PMSZ_OK;
+    }
+    ~EventTimer() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+// Pinned host memory for per-sweep counter read-back, one block per thread.
+void *host_pinned(size_t bytes);
+
+}  // namespace pmsz

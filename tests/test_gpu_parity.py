@@ -1,0 +1,205 @@
+"""GPU parity: every CUDA entry point, called through the C ABI, against the
+CPU oracle on the same seeded inputs.  Integer / index / field outputs must be
+bit-identical; counts per sweep must be equal."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pmsz_anonymous_gb300 import capi, fields as F
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def api():
+    from pmsz_anonymous_gb300 import api as A
+    return A
+
+
+def _dev(a, device):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+def _case(shape, dtype, comp, eb, seed, octaves=4, base=1 / 16):
+    f = F.perlin_field(shape, seed, octaves, base, dtype=dtype)
+    return f, F.standin(f, eb, comp, seed)
+
+
+def _flat_targets(codes, shape, nibble):
+    nz, ny, nx = shape
+    off = api().rank_offsets()
+    r = (codes >> 4) if nibble else (codes & 15)
+    r = r.astype(np.int64).ravel()
+    i = np.arange(r.size, dtype=np.int64)
+    return i + off[r, 0] + nx * (off[r, 1] + ny * off[r, 2])
+
+
+CASES = [
+    ((16, 16, 16), np.float32, "sz3", 1e-3, 0),
+    ((16, 16, 16), np.float32, "zfp", 1e-3, 1),
+    ((12, 20, 24), np.float64, "zfp", 1e-3, 2),
+    ((12, 20, 24), np.float64, "sz3", 2e-3, 3),
+    ((5, 17, 33), np.float32, "zfp", 5e-3, 4),     # nx not a multiple of 32
+    ((3, 7, 70), np.float64, "sz3", 1e-2, 5),      # three words per row, ragged tail
+    ((1, 1, 64), np.float32, "zfp", 5e-2, 6),      # a line
+    ((40, 1, 1), np.float64, "zfp", 5e-2, 7),      # a column along z
+    ((2, 2, 2), np.float32, "zfp", 1e-1, 8),
+    ((32, 32, 32), np.float32, "sz3", 1e-3, 9),
+    ((24, 24, 24), np.float64, "zfp", 1e-4, 10),
+]
+
+
+@pytest.mark.parametrize("full", [False, True])
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{np.dtype(c[1]).name}-{c[2]}" if isinstance(c, tuple) else str(c))
+def test_correct_matches_oracle(cuda, case, full):
+    shape, dtype, comp, eb, seed = case
+    f, fh = _case(shape, dtype, comp, eb, seed)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    df, dfh = _dev(f, cuda), _dev(fh, cuda)
+    r = api().correct(df, dfh, eb, full_sweeps=full)
+    out = dfh.cpu().numpy()
+    assert r.status == st
+    assert r.sweeps == sw
+    assert r.iteration == sw + 1
+    np.testing.assert_array_equal(out.view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
+    assert r.edits == int(recs[:, 3].sum())
+
+
+def test_active_set_covers_only_a_fraction(cuda):
+    f, fh = _case((32, 32, 32), np.float32, "zfp", 1e-3, 21)
+    r = api().correct(_dev(f, cuda), _dev(fh, cuda), 1e-3)
+    assert r.log[0, 6] == f.size            # sweep 1 is a full pass
+    if r.sweeps > 2:
+        assert r.log[1:, 6].max() < f.size  # later sweeps examine the active set only
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_codes_match_oracle_labels(cuda, dtype):
+    rng = np.random.default_rng(1)
+    f = rng.integers(0, 5, size=(9, 11, 37)).astype(dtype)   # plateaus: index tie-breaks
+    c = api().codes(_dev(f, cuda)).cpu().numpy()
+    asc, desc = O.label(f)
+    np.testing.assert_array_equal(_flat_targets(c, f.shape, 0), asc)
+    np.testing.assert_array_equal(_flat_targets(c, f.shape, 1), desc)
+
+
+def test_negative_zero_and_infinities(cuda):
+    f = np.array([0.0, -0.0, 0.0, -0.0, np.inf, -np.inf, 1.0, -1.0], np.float64).reshape(2, 2, 2)
+    c = api().codes(_dev(f, cuda)).cpu().numpy()
+    asc, desc = O.label(f)
+    np.testing.assert_array_equal(_flat_targets(c, f.shape, 0), asc)
+    np.testing.assert_array_equal(_flat_targets(c, f.shape, 1), desc)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_labels_match_path_compression(cuda, dtype):
+    f = F.perlin_field((20, 24, 28), 4, 4, 1 / 8, dtype=dtype)
+    c = api().codes(_dev(f, cuda))
+    a, d = api().labels(c)
+    asc, desc = O.label(f)
+    np.testing.assert_array_equal(a.cpu().numpy().ravel(), O.path_compress(asc))
+    np.testing.assert_array_equal(d.cpu().numpy().ravel(), O.path_compress(desc))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_verify_matches_oracle(cuda, dtype):
+    eb = 1e-3
+    f, fh = _case((16, 18, 20), dtype, "zfp", eb, 12)
+    got = api().verify(_dev(f, cuda), _dev(fh, cuda), eb)
+    ref = O.verify(f, fh, eb)
+    assert got["dir_mismatch"] == ref["dir_mismatch"] > 0
+    assert got["ext_mismatch"] == ref["ext_mismatch"]
+    assert got["as_mismatch"] == ref["as_mismatch"]
+    assert got["ds_mismatch"] == ref["ds_mismatch"]
+    assert got["bound_strict"] == ref["bound_violations"]
+    out, *_ = O.correct(f, fh, eb)
+    got = api().verify(_dev(f, cuda), _dev(out, cuda), eb)
+    assert got["dir_mismatch"] == got["as_mismatch"] == got["ds_mismatch"] == got["bound_beyond_clamp"] == 0
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_extract_edits_match_oracle(cuda, dtype):
+    eb = 1e-3
+    f, fh = _case((20, 21, 22), dtype, "sz3", eb, 13)
+    out, *_ = O.correct(f, fh, eb)
+    d, cl, ec = api().extract_edits(_dev(fh, cuda), _dev(out, cuda), _dev(f, cuda), eb)
+    rd, rcl, rec = O.extract_edits(fh, out, f, eb)
+    np.testing.assert_array_equal(d.cpu().numpy(), rd)
+    np.testing.assert_array_equal(cl.cpu().numpy().view(np.uint8), rcl.view(np.uint8))
+    assert ec == rec
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_generators_bit_exact(cuda, dtype):
+    shape = (7, 9, 11)
+    g = api().gen_perlin(shape, 3, 4, 1 / 8, 0.5, 2.0, dtype=torch.float32 if dtype == np.float32 else torch.float64)
+    ref = F.perlin_field(shape, 3, 4, 1 / 8, 0.5, 2.0, dtype=dtype)
+    np.testing.assert_array_equal(g.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    for comp in ("sz3", "zfp"):
+        s = api().standin(g, 1e-3, comp, seed=5)
+        np.testing.assert_array_equal(s.cpu().numpy().view(np.uint8), F.standin(ref, 1e-3, comp, 5).view(np.uint8))
+
+
+def test_nan_input_is_rejected(cuda):
+    f, fh = _case((8, 8, 8), np.float32, "zfp", 1e-3, 14)
+    fh[3, 3, 3] = np.nan
+    with pytest.raises(capi.PmszError) as e:
+        api().correct(_dev(f, cuda), _dev(fh, cuda), 1e-3)
+    assert e.value.status == capi.PMSZ_ERR_ARG
+
+
+def test_sentinel_value_is_rejected_fp64(cuda):
+    f, fh = _case((8, 8, 8), np.float64, "zfp", 1e-3, 15)
+    f[0, 0, 0] = 1e30
+    with pytest.raises(capi.PmszError):
+        api().correct(_dev(f, cuda), _dev(fh, cuda), 1e-3)
+
+
+def test_argument_errors(cuda):
+    f, fh = _case((4, 4, 4), np.float32, "zfp", 1e-3, 16)
+    with pytest.raises(capi.PmszError) as e:
+        api().correct(_dev(f, cuda), _dev(fh, cuda), -1.0)
+    assert e.value.status == capi.PMSZ_ERR_ARG
+    with pytest.raises(capi.PmszError):
+        api().correct(_dev(f, cuda), _dev(fh, cuda), 1e-3, q=0)
+
+
+def test_isolated_voxel_not_converged(cuda):
+    f = np.array([[[0.3]]], np.float64)
+    ref, cnt, st, sw, recs = O.correct(f, f.copy(), 0.1)
+    d = _dev(f.copy(), cuda)
+    r = api().correct(_dev(f, cuda), d, 0.1)
+    assert r.status == capi.PMSZ_ERR_NOT_CONVERGED == st
+    assert r.sweeps == sw
+    np.testing.assert_array_equal(d.cpu().numpy(), ref)
+
+
+def test_max_sweeps_cap(cuda):
+    f, fh = _case((16, 16, 16), np.float32, "zfp", 1e-3, 1)
+    r = api().correct(_dev(f, cuda), _dev(fh, cuda), 1e-3, max_sweeps=2)
+    assert r.status == capi.PMSZ_ERR_NOT_CONVERGED and r.sweeps == 2
+
+
+def test_repeat_is_bit_identical(cuda):
+    f, fh = _case((24, 24, 24), np.float64, "zfp", 1e-4, 17)
+    outs = []
+    for _ in range(2):
+        d = _dev(fh, cuda)
+        api().correct(_dev(f, cuda), d, 1e-4)
+        outs.append(d.cpu().numpy())
+    np.testing.assert_array_equal(outs[0].view(np.uint8), outs[1].view(np.uint8))
+
+
+def test_medium_field_against_oracle(cuda):
+    """128^3 fp64 through the device generator, checked against the oracle."""
+    shape, eb = (128, 128, 128), 1e-4
+    df = api().gen_perlin(shape, 1, 5, 1 / 64, dtype=torch.float64)
+    dfh = api().standin(df, eb, "zfp", 1)
+    f, fh = df.cpu().numpy(), dfh.cpu().numpy()
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    r = api().correct(df, dfh, eb)
+    assert r.status == st == capi.PMSZ_OK
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)

@@ -1,0 +1,95 @@
+"""CPU tests of the native library that need no GPU: it loads, exports every
+symbol the headers declare, and its host encoder matches the oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pmsz_anonymous_gb300 import _build, capi, fields as F
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return capi.load()
+
+
+def _declared():
+    names = set()
+    for h in ("pmsz.h", "pmsz_host.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(pmsz_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for n in sorted(names):
+        assert hasattr(lib, n), f"{n} declared in include/ but not exported"
+    assert set(capi.SIGNATURES) == names
+
+
+def test_status_strings(lib):
+    assert lib.pmsz_strerror(0) == b"ok"
+    assert lib.pmsz_strerror(3) == b"not converged"
+    assert lib.pmsz_version() >= 100
+
+
+def test_argument_errors_without_gpu(lib):
+    # null pointers and bad sizes are rejected before any CUDA call
+    assert lib.pmsz_correct_f32(None, None, 4, 4, 4, 1e-3, None, None, None) == capi.PMSZ_ERR_ARG
+    assert b"null" in lib.pmsz_last_error()
+
+
+def test_delta_encoder_matches_oracle_pack(lib):
+    from pmsz_anonymous_gb300 import api
+    rng = np.random.default_rng(0)
+    d = rng.integers(0, 6, 10007).astype(np.uint8)
+    blob = api.encode_deltas(d, 5)
+    np.testing.assert_array_equal(api.decode_deltas(blob, d.size, 5), d)
+    # the payload inside the zstd frame is the oracle's 3-bit pack
+    import ctypes
+    L = ctypes.CDLL("libzstd.so.1")
+    L.ZSTD_decompress.restype = ctypes.c_size_t
+    L.ZSTD_decompress.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]
+    packed = O.pack_nbits(d, 3)
+    buf = ctypes.create_string_buffer(len(packed))
+    n = L.ZSTD_decompress(buf, len(packed), blob, len(blob))
+    assert n == len(packed) and buf.raw == packed
+
+
+def test_clamp_encoder_round_trip(lib):
+    from pmsz_anonymous_gb300 import api
+    assert api.encode_clamps(np.zeros(0, np.float64)) == b""
+    v = np.linspace(-1, 1, 999).astype(np.float32)
+    np.testing.assert_array_equal(api.decode_clamps(api.encode_clamps(v), np.float32), v)
+    assert api.zstd_version() >= 10500
+
+
+def test_rank_table(lib):
+    from pmsz_anonymous_gb300 import api
+    off = api.rank_offsets()
+    # lexicographic (dz, dy, dx) order, centre at rank 7, opposite ranks r / 14-r
+    keys = [tuple(o[::-1]) for o in off]
+    assert keys == sorted(keys)
+    assert tuple(off[7]) == (0, 0, 0)
+    for r in range(15):
+        assert tuple(off[r]) == tuple(-off[14 - r])
+    # the 14 non-centre offsets are the reference's stencil (pMSz.cu:186-193)
+    from tests import refpy
+    assert {tuple(o) for i, o in enumerate(off) if i != 7} == set(refpy.DIRS)
+
+
+def test_fields_are_normalised_and_bounded():
+    f = F.perlin_field((8, 9, 10), 0, 4, 1 / 32, dtype=np.float32)
+    assert f.dtype == np.float32 and f.min() == 0.0 and f.max() == 1.0
+    for comp in ("sz3", "zfp"):
+        fh = F.standin(f, 1e-3, comp)
+        assert np.all(np.abs(f - fh) <= np.float32(1e-3))
+    assert np.array_equal(F.perlin_field((4, 5, 6), 3, 2, 0.1), F.perlin_field((4, 5, 6), 3, 2, 0.1))
