@@ -69,6 +69,10 @@ typedef struct pmsz_result {
      * all edit passes; launches = kernels launched by the call. */
     double ms_first_pass, ms_detect, ms_apply;
     int64_t launches;
+    /* Device milliseconds from the first to the last kernel of the loop
+     * (always measured): the window of the reference's "comfputational
+     * overhead" print, pMSz.cu:2905-2950. */
+    double ms_total;
 } pmsz_result;
 
 /* Verification counts (replaces the reference's disabled check_consistency

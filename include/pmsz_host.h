@@ -37,6 +37,29 @@ int pmsz_decode_clamps(const uint8_t *comp, size_t len, size_t elem_size, void *
 
 void pmsz_free(void *p);
 
+/* Optional outputs of pmsz_correct_host_*. */
+typedef struct pmsz_host_outputs {
+    uint8_t *deltas;             /* host array of n bytes: edit symbols, or NULL */
+    void *clamp;                 /* host array of n values of the field type, or NULL;
+                                    the first n_clamp entries are the clamp list */
+    uint64_t n_clamp;            /* out */
+    uint64_t edit_count;         /* out: voxels with cur < prev, the reference's "Edit count" */
+    pmsz_verify_result *verify;  /* re-verification of the result, or NULL */
+} pmsz_host_outputs;
+
+/*
+ * pmsz_correct_host_{f32,f64}: the reference main's single-rank pipeline
+ * (pMSz.cu:2855-2987: device copies, c_loops, gather_cost_sparse) on HOST
+ * arrays.  f and fhat are host arrays of nx*ny*nz values; fhat is replaced by
+ * the corrected field.  outs may be NULL.  Device memory is allocated
+ * stream-ordered on `stream` (a cudaStream_t, NULL = default stream) and
+ * released before return.  Same status codes as pmsz_correct_*.
+ */
+int pmsz_correct_host_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                          const pmsz_opts *opts, pmsz_result *res, pmsz_host_outputs *outs, void *stream);
+int pmsz_correct_host_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                          const pmsz_opts *opts, pmsz_result *res, pmsz_host_outputs *outs, void *stream);
+
 /* ZSTD_versionNumber() of the libzstd the library loaded (byte parity of the
  * edit files holds only for equal zstd versions). */
 unsigned pmsz_zstd_version(void);

@@ -25,7 +25,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libpmsz_gb300.so")
 CLI = os.path.join(LIBDIR, "pmsz")
 
-CUDA_SOURCES = ["support.cu", "correct.cu", "verify.cu", "edits.cu", "gen.cu"]
+CUDA_SOURCES = ["support.cu", "correct.cu", "verify.cu", "edits.cu", "gen.cu", "host.cu"]
 CXX_SOURCES = ["encode.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -82,8 +82,12 @@ def build(verbose: bool = False) -> str:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     cli_src = os.path.join(CSRC, "cli.cpp")
     if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB, *_headers()]):
-        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", f"-I{INCLUDE}", cli_src, "-o", CLI,
-               f"-L{LIBDIR}", "-lpmsz_gb300", "-Wl,-rpath,$ORIGIN"]
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+        cudalib = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"))
+                        if os.path.exists(os.path.join(d, "libcudart.so"))), os.path.join(cuda, "lib64"))
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", f"-I{INCLUDE}", f"-I{os.path.join(cuda, 'include')}",
+               cli_src, "-o", CLI, f"-L{LIBDIR}", "-lpmsz_gb300", f"-L{cudalib}", "-lcudart",
+               f"-Wl,-rpath,$ORIGIN:{cudalib}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -54,6 +54,7 @@ class CorrectResult:
     ms_detect: float = 0.0
     ms_apply: float = 0.0
     launches: int = 0
+    ms_total: float = 0.0
 
     @property
     def converged(self) -> bool:
@@ -84,7 +85,7 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
     rows = np.array([[getattr(log[i], k) for k in SWEEP_KEYS] for i in range(n)],
                     dtype=np.uint64).reshape(n, len(SWEEP_KEYS))
     return CorrectResult(st, n, int(res.iteration), int(res.edits), rows, float(res.ms_first_pass),
-                         float(res.ms_detect), float(res.ms_apply), int(res.launches))
+                         float(res.ms_detect), float(res.ms_apply), int(res.launches), float(res.ms_total))
 
 
 def codes(v: torch.Tensor, stream=None) -> torch.Tensor:

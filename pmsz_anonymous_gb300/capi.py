@@ -33,12 +33,17 @@ class Result(ctypes.Structure):
     _fields_ = [("sweeps", c_i64), ("iteration", c_i64), ("edits", c_u64),
                 ("sweep_log", ctypes.POINTER(SweepRecord)), ("sweep_log_cap", c_i64),
                 ("ms_first_pass", c_double), ("ms_detect", c_double), ("ms_apply", c_double),
-                ("launches", c_i64)]
+                ("launches", c_i64), ("ms_total", c_double)]
 
 
 class VerifyResult(ctypes.Structure):
     _fields_ = [("dir_mismatch", c_u64), ("ext_mismatch", c_u64), ("as_mismatch", c_u64),
                 ("ds_mismatch", c_u64), ("bound_strict", c_u64), ("bound_beyond_clamp", c_u64)]
+
+
+class HostOutputs(ctypes.Structure):
+    _fields_ = [("deltas", c_void_p), ("clamp", c_void_p), ("n_clamp", c_u64), ("edit_count", c_u64),
+                ("verify", ctypes.POINTER(VerifyResult))]
 
 
 # name -> (restype, argtypes), one line per declaration in include/*.h
@@ -67,6 +72,8 @@ SIGNATURES = {
     "pmsz_decode_clamps": (c_int, [_P, c_size, c_size, _P, _P]),
     "pmsz_free": (None, [_P]),
     "pmsz_zstd_version": (c_u32, []),
+    "pmsz_correct_host_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
+    "pmsz_correct_host_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -314,6 +314,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint32_t *req = ws.at<uint32_t>(o_req);
     uint32_t *act[2] = {ws.at<uint32_t>(o_a0), ws.at<uint32_t>(o_a1)};
     SweepSlot *slots = ws.at<SweepSlot>(o_slots);
+    EventTimer et;
+    if ((rc = et.init())) return rc;
+    PMSZ_CUDA(cudaEventRecord(et.ev[3], s));  // start of the loop's device window
 
     PMSZ_CUDA(cudaMemsetAsync(cnt, 0, g.n, s));  // init_counter, pMSz.cu:1745-1749
     PMSZ_CUDA(cudaMemsetAsync(req, 0, g.nwords * 4, s));
@@ -324,8 +327,6 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     SweepSlot *hslot = static_cast<SweepSlot *>(host_pinned(sizeof(SweepSlot)));
     if (!hslot) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
     const bool timing = (flags & PMSZ_FLAG_TIMING) != 0;
-    EventTimer et;
-    if (timing && (rc = et.init())) return rc;
     double ms_first = 0, ms_detect = 0, ms_apply = 0;
     int64_t launches = 0;
     const dim3 blk3(32, 8, 1);
@@ -374,6 +375,10 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         cur ^= 1;
     }
+    float ms_total = 0;
+    PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+    PMSZ_CUDA(cudaEventSynchronize(et.ev[0]));
+    PMSZ_CUDA(cudaEventElapsedTime(&ms_total, et.ev[3], et.ev[0]));
     if (status == PMSZ_ERR_NOT_CONVERGED && sweeps >= max_sweeps)
         set_error(PMSZ_ERR_NOT_CONVERGED, "max_sweeps reached before convergence");
     if (res) {
@@ -384,6 +389,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         res->ms_detect = ms_detect;
         res->ms_apply = ms_apply;
         res->launches = launches;
+        res->ms_total = ms_total;
         if (res->sweep_log && res->sweep_log_cap > 0) {
             const size_t m = std::min<size_t>(log.size(), static_cast<size_t>(res->sweep_log_cap));
             static_assert(sizeof(SweepSlot) == sizeof(pmsz_sweep_record), "record layout");
@@ -407,6 +413,9 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
 
 template int codes_impl<float>(const float *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
 template int codes_impl<double>(const double *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
+
+template int correct_impl<float>(const float *, float *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t);
+template int correct_impl<double>(const double *, double *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t);
 
 }  // namespace pmsz
 

@@ -130,8 +130,6 @@ __global__ void __launch_bounds__(256) k_scatter_clamps(const T *__restrict__ cu
     }
 }
 
-int check_geom(size_t nx, size_t ny, size_t nz);
-
 template <typename T>
 int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas, T *clamp,
                  uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s) {
@@ -164,6 +162,9 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
     *edit_count = h[1];
     return ws.release();
 }
+
+template int extract_impl<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *, float *, uint64_t *, uint64_t *, cudaStream_t);
+template int extract_impl<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *, double *, uint64_t *, uint64_t *, cudaStream_t);
 
 }  // namespace pmsz
 

@@ -136,8 +136,6 @@ __global__ void __launch_bounds__(256) k_standin(const T *__restrict__ f, T *__r
     }
 }
 
-int check_geom(size_t nx, size_t ny, size_t nz);
-
 template <typename T>
 int perlin_impl(T *out, size_t nx, size_t ny, size_t nz, const int32_t *perm, const double *amps,
                 const double *freqs, int octaves, cudaStream_t s) {

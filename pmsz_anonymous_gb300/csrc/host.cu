@@ -1,0 +1,68 @@
+// host.cu -- host-buffer entry points: the reference's main-program pipeline
+// for one rank (pMSz.cu:2855-2987) behind one call.  The caller hands HOST
+// arrays; the call copies f and fhat to the device, keeps the pre-correction
+// copy the reference keeps in device_decp_copy (pMSz.cu:2898), runs the
+// correction loop, and returns the corrected field plus, on request, the edit
+// output of gather_cost_sparse / run_extract_edits (pMSz.cu:2429-2543,
+// 2140-2226) and a re-verification.  Device buffers are stream-ordered
+// allocations on `stream`, freed before return.
+#include "internal.h"
+
+#include <cstring>
+
+namespace pmsz {
+
+template <typename T>
+int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
+              pmsz_result *res, pmsz_host_outputs *outs, cudaStream_t s) {
+    if (!f || !fhat) return set_error(PMSZ_ERR_ARG, "null field pointer");
+    if (nx == 0 || ny == 0 || nz == 0) return set_error(PMSZ_ERR_ARG, "field dimensions must be positive");
+    const size_t n = nx * ny * nz;
+    const bool want_edits = outs && (outs->deltas || outs->clamp);
+    const bool want_verify = outs && outs->verify;
+    const int q = opts ? opts->q : 5;
+    Workspace ws(s);
+    const size_t o_f = ws.reserve<T>(n), o_fh = ws.reserve<T>(n);
+    const size_t o_prev = ws.reserve<T>(want_edits ? n : 0);
+    const size_t o_d = ws.reserve<uint8_t>(want_edits ? n : 0);
+    const size_t o_c = ws.reserve<T>(want_edits ? n : 0);
+    int rc = ws.commit();
+    if (rc) return rc;
+    T *df = ws.at<T>(o_f), *dfh = ws.at<T>(o_fh), *dprev = ws.at<T>(o_prev), *dclamp = ws.at<T>(o_c);
+    uint8_t *dd = ws.at<uint8_t>(o_d);
+    PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    PMSZ_CUDA(cudaMemcpyAsync(dfh, fhat, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    if (want_edits) PMSZ_CUDA(cudaMemcpyAsync(dprev, dfh, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    const int st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
+    if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
+    std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
+    if (want_edits) {
+        uint64_t nc = 0, ec = 0;
+        if ((rc = extract_impl<T>(dprev, dfh, df, n, eb, q, dd, dclamp, &nc, &ec, s))) return rc;
+        outs->n_clamp = nc;
+        outs->edit_count = ec;
+        if (outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        if (outs->clamp && nc) PMSZ_CUDA(cudaMemcpyAsync(outs->clamp, dclamp, nc * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    if (want_verify && (rc = verify_impl<T>(df, dfh, nx, ny, nz, eb, outs->verify, s))) return rc;
+    PMSZ_CUDA(cudaMemcpyAsync(fhat, dfh, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    PMSZ_CUDA(cudaStreamSynchronize(s));
+    if ((rc = ws.release())) return rc;
+    if (st == PMSZ_ERR_NOT_CONVERGED) set_error(st, keep);
+    return st;
+}
+
+}  // namespace pmsz
+
+using namespace pmsz;
+
+extern "C" int pmsz_correct_host_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                                     const pmsz_opts *opts, pmsz_result *res, pmsz_host_outputs *outs,
+                                     void *stream) {
+    return guarded([&] { return host_impl<float>(f, fhat, nx, ny, nz, eb, opts, res, outs, as_stream(stream)); });
+}
+extern "C" int pmsz_correct_host_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz, double eb,
+                                     const pmsz_opts *opts, pmsz_result *res, pmsz_host_outputs *outs,
+                                     void *stream) {
+    return guarded([&] { return host_impl<double>(f, fhat, nx, ny, nz, eb, opts, res, outs, as_stream(stream)); });
+}

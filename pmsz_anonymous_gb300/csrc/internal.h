@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/pmsz.h"
+#include "../../include/pmsz_host.h"
 
 namespace pmsz {
 
@@ -87,5 +88,20 @@ struct EventTimer {
 
 // Pinned host memory for per-sweep counter read-back, one block per thread.
 void *host_pinned(size_t bytes);
+
+// Implementations behind the C entry points (explicitly instantiated for
+// float and double in their translation units).
+int check_geom(size_t nx, size_t ny, size_t nz);
+template <typename T>
+int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
+                 pmsz_result *res, cudaStream_t s);
+template <typename T>
+int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cudaStream_t s);
+template <typename T>
+int verify_impl(const T *f, const T *fp, size_t nx, size_t ny, size_t nz, double eb, pmsz_verify_result *out,
+                cudaStream_t s);
+template <typename T>
+int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas, T *clamp,
+                 uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s);
 
 }  // namespace pmsz

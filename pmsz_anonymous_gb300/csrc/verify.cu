@@ -16,8 +16,6 @@
 
 namespace pmsz {
 
-int check_geom(size_t nx, size_t ny, size_t nz);
-
 __global__ void __launch_bounds__(256) k_init_ptr(const uint8_t *__restrict__ codes, uint32_t *__restrict__ as,
                                                   uint32_t *__restrict__ ds, Geom g) {
     const int x = blockIdx.x * 32 + threadIdx.x;
@@ -118,9 +116,6 @@ __global__ void __launch_bounds__(256) k_count_diff(const uint32_t *__restrict__
 }
 
 template <typename T>
-int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cudaStream_t s);
-
-template <typename T>
 int verify_impl(const T *f, const T *fp, size_t nx, size_t ny, size_t nz, double eb, pmsz_verify_result *out,
                 cudaStream_t s) {
     if (!f || !fp || !out) return set_error(PMSZ_ERR_ARG, "null pointer");
@@ -162,6 +157,9 @@ int verify_impl(const T *f, const T *fp, size_t nx, size_t ny, size_t nz, double
     out->bound_beyond_clamp = h[5];
     return ws.release();
 }
+
+template int verify_impl<float>(const float *, const float *, size_t, size_t, size_t, double, pmsz_verify_result *, cudaStream_t);
+template int verify_impl<double>(const double *, const double *, size_t, size_t, size_t, double, pmsz_verify_result *, cudaStream_t);
 
 }  // namespace pmsz
 
