@@ -111,6 +111,34 @@ int pmsz_correct_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t
                      double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
 
 /*
+ * pmsz_correct_noalloc: the same correction as pmsz_correct_{f32,f64}, but
+ * without allocating any memory -- for callers that cannot call cudaMalloc or
+ * a caching allocator while they run, typically because another component
+ * already owns the GPU's memory (an in-situ pipeline inside a simulation that
+ * reserved HBM up front, a service with a fixed memory budget) or because an
+ * allocator call is not acceptable on their path.  It has no counterpart in
+ * the reference.  elem_size selects the field type: 4 = float, 8 = double.
+ * The caller passes the fields as for pmsz_correct_*; every other buffer is a
+ * fixed array inside the library image (PMSZ_NOALLOC_SCRATCH_BYTES, about
+ * 5.75 MiB), which every GPU that loads the library holds until the process
+ * exits.  Limits, rejected with PMSZ_ERR_ARG and a message: nx*ny*nz <=
+ * PMSZ_NOALLOC_MAX_VOXELS (2^21, e.g. 128^3), ceil(nx/32)*ny*nz <=
+ * PMSZ_NOALLOC_MAX_WORDS, max_sweeps <= PMSZ_NOALLOC_MAX_SWEEPS (also the
+ * default).  The first call on a device looks up the array's device address
+ * with that device current; make that first call before any stream capture.
+ * All calls on a device share the array and every call clears what must
+ * start at zero, so calls that overlap on the GPU (two streams, or two host
+ * threads) race: serialise them.  PMSZ_FLAG_TIMING is ignored; the ms_*
+ * fields of res are set to 0.
+ */
+#define PMSZ_NOALLOC_MAX_VOXELS 2097152u
+#define PMSZ_NOALLOC_MAX_WORDS 131072u
+#define PMSZ_NOALLOC_MAX_SWEEPS 4096u
+#define PMSZ_NOALLOC_SCRATCH_BYTES (2u * PMSZ_NOALLOC_MAX_VOXELS + 12u * PMSZ_NOALLOC_MAX_WORDS + 64u * PMSZ_NOALLOC_MAX_SWEEPS)
+int pmsz_correct_noalloc(const void *f, void *fhat, size_t elem_size, size_t nx, size_t ny, size_t nz,
+                         double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
+
+/*
  * pmsz_codes_{f32,f64}: steepest-direction labelling of one field -- the
  * neighbour scan and or_types encoding of iscriticle data_type=1
  * (pMSz.cu:686-783).  codes[i] (device, n bytes): low nibble = stencil rank of

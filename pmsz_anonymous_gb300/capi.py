@@ -72,6 +72,7 @@ SIGNATURES = {
     "pmsz_decode_clamps": (c_int, [_P, c_size, c_size, _P, _P]),
     "pmsz_free": (None, [_P]),
     "pmsz_zstd_version": (c_u32, []),
+    "pmsz_correct_noalloc": (c_int, [_P, _P, c_size, c_size, c_size, c_size, c_double, _P, _P, _P]),
     "pmsz_correct_host_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
     "pmsz_correct_host_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
 }

@@ -24,6 +24,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 namespace pmsz {
@@ -441,4 +443,156 @@ extern "C" int pmsz_rank_offset(int r, int *dx, int *dy, int *dz) {
     *dy = rank_dy(r);
     *dz = rank_dz(r);
     return PMSZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pmsz_correct_noalloc: the correction loop with its scratch in a fixed
+// device array instead of per-call allocations, for callers that must not
+// allocate device memory -- code that runs while another component owns the
+// GPU's memory through its own pool or arena (a simulation that reserved HBM
+// up front for in-situ compression, a serving process with a fixed budget),
+// or that cannot afford an allocator call on its path.  The array below is
+// part of the library image: every GPU that loads the library holds its
+// PMSZ_NOALLOC_SCRATCH_BYTES until the process exits, and all calls on a
+// device share it.
+// ---------------------------------------------------------------------------
+namespace pmsz {
+namespace noalloc {
+
+constexpr size_t kMaxVoxels = PMSZ_NOALLOC_MAX_VOXELS;
+constexpr size_t kMaxWords = PMSZ_NOALLOC_MAX_WORDS;
+constexpr size_t kMaxSweeps = PMSZ_NOALLOC_MAX_SWEEPS;
+constexpr size_t kOffCodes = 0;
+constexpr size_t kOffCnt = kOffCodes + kMaxVoxels;
+constexpr size_t kOffReq = kOffCnt + kMaxVoxels;
+constexpr size_t kOffAct0 = kOffReq + 4 * kMaxWords;
+constexpr size_t kOffAct1 = kOffAct0 + 4 * kMaxWords;
+constexpr size_t kOffSlots = kOffAct1 + 4 * kMaxWords;
+constexpr size_t kBytes = kOffSlots + sizeof(SweepSlot) * kMaxSweeps;
+static_assert(kBytes == PMSZ_NOALLOC_SCRATCH_BYTES, "header constant out of date");
+static_assert(kOffReq % 256 == 0 && kOffSlots % 256 == 0, "sub-arrays stay 256-byte aligned");
+
+// codes | edit counters | request bitmap | two active bitmaps | sweep slots
+static __device__ __align__(256) unsigned char g_scratch[kBytes];
+
+// Host-side address of g_scratch per device, looked up once per device with
+// that device current (the host symbol itself is not a device address).
+constexpr int kMaxDevices = 64;
+static std::mutex g_mu;
+static unsigned char *g_addr[kMaxDevices] = {};
+
+static int scratch_address(unsigned char **out) {
+    int dev = 0;
+    PMSZ_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(PMSZ_ERR_ARG, "device ordinal beyond the supported range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        void *p = nullptr;
+        PMSZ_CUDA(cudaGetSymbolAddress(&p, g_scratch));
+        g_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_addr[dev];
+    return PMSZ_OK;
+}
+
+template <typename T>
+int run(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts, pmsz_result *res,
+        cudaStream_t s) {
+    if (!f || !fh) return set_error(PMSZ_ERR_ARG, "null field pointer");
+    int rc = check_geom(nx, ny, nz);
+    if (rc) return rc;
+    const int q = opts ? opts->q : 5;
+    const uint32_t flags = opts ? opts->flags : 0u;
+    const int64_t max_sweeps = opts && opts->max_sweeps > 0 ? opts->max_sweeps : static_cast<int64_t>(kMaxSweeps);
+    if (!(eb > 0.0) || !(eb < 1e300)) return set_error(PMSZ_ERR_ARG, "error bound must be positive and finite");
+    if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
+    const Geom g = make_geom(nx, ny, nz);
+    if (g.n > kMaxVoxels)
+        return set_error(PMSZ_ERR_ARG, "pmsz_correct_noalloc: field of " + std::to_string(g.n) +
+                                           " voxels exceeds its fixed scratch (at most " + std::to_string(kMaxVoxels) +
+                                           " voxels); use pmsz_correct_f32/f64");
+    if (g.nwords > kMaxWords)
+        return set_error(PMSZ_ERR_ARG, "pmsz_correct_noalloc: ceil(nx/32)*ny*nz = " + std::to_string(g.nwords) +
+                                           " exceeds its fixed bitmap scratch (at most " + std::to_string(kMaxWords) + ")");
+    if (max_sweeps > static_cast<int64_t>(kMaxSweeps))
+        return set_error(PMSZ_ERR_ARG, "pmsz_correct_noalloc: max_sweeps above " + std::to_string(kMaxSweeps));
+    unsigned char *base = nullptr;
+    if ((rc = scratch_address(&base))) return rc;
+    uint8_t *codes = base + kOffCodes;
+    uint8_t *cnt = base + kOffCnt;
+    uint32_t *req = reinterpret_cast<uint32_t *>(base + kOffReq);
+    uint32_t *act[2] = {reinterpret_cast<uint32_t *>(base + kOffAct0), reinterpret_cast<uint32_t *>(base + kOffAct1)};
+    SweepSlot *slots = reinterpret_cast<SweepSlot *>(base + kOffSlots);
+
+    // The array keeps the previous call's contents: clear everything that
+    // the loop expects to start at zero (codes are fully rewritten by sweep 1).
+    PMSZ_CUDA(cudaMemsetAsync(cnt, 0, g.n, s));
+    PMSZ_CUDA(cudaMemsetAsync(req, 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
+    PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
+
+    const T eps = static_cast<T>(eb);
+    const T delta = static_cast<T>(eb / static_cast<double>(q));
+    const dim3 blk3(32, 8, 1);
+    int cur = 0;
+    int64_t sweeps = 0;
+    uint64_t edits = 0;
+    int status = PMSZ_ERR_NOT_CONVERGED;
+    while (sweeps < max_sweeps) {
+        SweepSlot *slot = slots + sweeps;
+        uint32_t *a_next = act[cur ^ 1];
+        if (sweeps == 0) {
+            k_detect_full<T, true><<<grid3(g), blk3, 0, s>>>(f, fh, codes, req, a_next, slot, g);
+        } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
+            k_detect_full<T, false><<<grid3(g), blk3, 0, s>>>(nullptr, fh, codes, req, a_next, slot, g);
+        } else {
+            k_detect_sparse<T><<<stride_grid(g.nwords), 256, 0, s>>>(fh, codes, act[cur], a_next, req, slot, g);
+        }
+        k_apply<T><<<stride_grid(g.nwords), 256, 0, s>>>(f, fh, cnt, req, a_next, slot, g, eps, delta, q);
+        PMSZ_CUDA(cudaGetLastError());
+        SweepSlot h;  // read back into the caller's stack: no pinned buffer
+        PMSZ_CUDA(cudaMemcpyAsync(&h, slot, sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        if (res && res->sweep_log && sweeps < res->sweep_log_cap)
+            std::memcpy(res->sweep_log + sweeps, &h, sizeof(SweepSlot));
+        ++sweeps;
+        edits += h.requested;
+        if (sweeps == 1 && h.bad) {
+            status = set_error(PMSZ_ERR_ARG, "input contains NaN or the value 1e30 (the reference's halo sentinel)");
+            break;
+        }
+        if (h.fmax == 0 && h.fmin == 0 && h.fdir == 0) { status = PMSZ_OK; break; }
+        if (h.progressed == 0) {
+            set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
+            break;
+        }
+        cur ^= 1;
+    }
+    if (status == PMSZ_ERR_NOT_CONVERGED && sweeps >= max_sweeps)
+        set_error(PMSZ_ERR_NOT_CONVERGED, "max_sweeps reached before convergence");
+    if (res) {
+        res->sweeps = sweeps;
+        res->iteration = sweeps + 1;
+        res->edits = edits;
+        res->ms_first_pass = res->ms_detect = res->ms_apply = res->ms_total = 0.0;
+        res->launches = 2 * sweeps;
+    }
+    return status;
+}
+
+}  // namespace noalloc
+}  // namespace pmsz
+
+extern "C" int pmsz_correct_noalloc(const void *f, void *fhat, size_t elem_size, size_t nx, size_t ny, size_t nz,
+                                    double eb, const pmsz_opts *opts, pmsz_result *res, void *stream) {
+    return guarded([&] {
+        if (elem_size == sizeof(float))
+            return noalloc::run<float>(static_cast<const float *>(f), static_cast<float *>(fhat), nx, ny, nz, eb,
+                                       opts, res, as_stream(stream));
+        if (elem_size == sizeof(double))
+            return noalloc::run<double>(static_cast<const double *>(f), static_cast<double *>(fhat), nx, ny, nz, eb,
+                                        opts, res, as_stream(stream));
+        return set_error(PMSZ_ERR_ARG, "elem_size must be 4 (float) or 8 (double)");
+    });
 }
