@@ -1,0 +1,61 @@
+"""Build recipe of the reference-kernel harness (test infrastructure only).
+
+* ``oracle/_ref/pmsz_ref.cubin`` -- the UNMODIFIED reference ``pMSz.cu``,
+  compiled where it lies (``/root/reference``) into sm_103a device code, with
+  the declaration-only headers of ``oracle/ref_shim`` standing in for MPI,
+  SZ3, ZFP and zstd (the cubin keeps only the kernels; nothing of those
+  libraries is called).  Built only where the reference sources exist; the
+  cubin then travels with the repository copy.
+* ``oracle/_ref/ref_harness`` -- ``oracle/ref_harness.cpp`` (driver API),
+  compiled on the machine that runs it.
+
+Everything lands in ``oracle/_ref/`` (git-ignored).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REF_SRC = "/root/reference/pMSz.cu"
+CUBIN = os.path.join(OUT, "pmsz_ref.cubin")
+HARNESS = os.path.join(OUT, "ref_harness")
+
+
+def _cuda_home() -> str:
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+
+
+def build_cubin() -> str | None:
+    if not os.path.exists(REF_SRC):
+        return CUBIN if os.path.exists(CUBIN) else None
+    os.makedirs(OUT, exist_ok=True)
+    if not os.path.exists(CUBIN) or os.path.getmtime(CUBIN) < os.path.getmtime(REF_SRC):
+        cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
+               "-std=c++17", "-I" + os.path.join(HERE, "ref_shim"), REF_SRC, "-o", CUBIN]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return CUBIN
+
+
+def build_harness() -> str:
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "ref_harness.cpp")
+    if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < os.path.getmtime(src):
+        cuda = _cuda_home()
+        libdir = next(d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"),
+                                  os.path.join(cuda, "targets", "sbsa-linux", "lib"))
+                      if os.path.isdir(os.path.join(d, "stubs")))
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I" + os.path.join(cuda, "include"), src,
+               "-o", HARNESS, "-L" + os.path.join(libdir, "stubs"), "-lcuda"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return HARNESS
+
+
+if __name__ == "__main__":
+    print(build_cubin())
+    if "--harness" in sys.argv:
+        print(build_harness())
