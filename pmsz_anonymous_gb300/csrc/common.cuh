@@ -128,13 +128,39 @@ __device__ __forceinline__ uint32_t detect_rules(int asc, int desc, int oasc, in
     return tm;
 }
 
+// Division by a run-time constant d >= 1 for 32-bit n, as a multiply and a
+// shift (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994): with s = ceil(log2 d) and
+// m = floor(2^32 (2^s - d) / d) + 1, floor(n / d) = (mulhi(n, m) + n) >> s.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t s = 0;
+    while ((uint64_t(1) << s) < d) ++s;
+    f.s = s;
+    f.m = static_cast<uint32_t>(((uint64_t(1) << 32) * ((uint64_t(1) << s) - d)) / d + 1);
+    return f;
+}
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+#ifdef __CUDA_ARCH__
+    const uint32_t t = __umulhi(n, f.m);
+#else
+    const uint32_t t = static_cast<uint32_t>((static_cast<uint64_t>(n) * f.m) >> 32);
+#endif
+    return static_cast<uint32_t>((static_cast<uint64_t>(t) + n) >> f.s);
+}
+
 // Field geometry.  Bitmaps hold one bit per voxel with every x-row padded to
 // whole 32-bit words: word (wx, y, z) = wx + wpr*(y + ny*z), bit b = x - 32*wx.
 struct Geom {
     int nx, ny, nz;
     int wpr;          // words per x-row
-    size_t nwords;    // wpr * ny * nz
+    size_t nwords;    // wpr * ny * nz (< 2^32)
     size_t n;         // nx * ny * nz
+    FastDiv div_wpr, div_ny;
 };
 
 inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
@@ -145,7 +171,19 @@ inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
     g.wpr = static_cast<int>((nx + 31) / 32);
     g.nwords = static_cast<size_t>(g.wpr) * ny * nz;
     g.n = nx * ny * nz;
+    g.div_wpr = make_fastdiv(static_cast<uint32_t>(g.wpr));
+    g.div_ny = make_fastdiv(static_cast<uint32_t>(ny));
     return g;
+}
+
+// (wx, y, z) of bitmap word w.
+__host__ __device__ __forceinline__ void word_coords(const Geom &g, size_t w, int &wx, int &y, int &z) {
+    const uint32_t w32 = static_cast<uint32_t>(w);
+    const uint32_t row = fdiv(w32, g.div_wpr);
+    wx = static_cast<int>(w32 - row * static_cast<uint32_t>(g.wpr));
+    const uint32_t zz = fdiv(row, g.div_ny);
+    y = static_cast<int>(row - zz * static_cast<uint32_t>(g.ny));
+    z = static_cast<int>(zz);
 }
 
 __host__ __device__ __forceinline__ size_t flat(const Geom &g, int x, int y, int z) {

@@ -268,6 +268,12 @@ __global__ void __launch_bounds__(256) k_codes(const T *__restrict__ v, uint8_t 
     codes[i] = static_cast<uint8_t>(a | (d << 4));
 }
 
+}  // namespace pmsz
+
+#include "tiled.cuh"
+
+namespace pmsz {
+
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
@@ -280,10 +286,58 @@ static inline unsigned stride_grid(size_t items) {
     return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(want, 152 * 16)));
 }
 
+// Runs sweeps first.. in one cooperative launch of k_sweep_loop (grid = the
+// number of co-resident blocks); *done receives the total number of sweeps.
+template <typename T>
+static int run_sweep_loop(const T *f, T *fh, const uint8_t *codes, uint8_t *cnt, uint32_t *hp, uint32_t *req,
+                          uint32_t *const act[2], SweepSlot *slots, int64_t first, int64_t max_sweeps, const Geom &g,
+                          T eps, T delta, int q, cudaStream_t s, EventTimer *et, double *ms_acc, int64_t *done) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    PMSZ_CUDA(cudaGetDevice(&dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return set_error(PMSZ_ERR_CUDA, "device does not support cooperative launches");
+    PMSZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_loop<T>, kListBlock, 0));
+    if (per_sm < 1) return set_error(PMSZ_ERR_CUDA, "sweep loop kernel does not fit on an SM");
+    const size_t need = (g.nwords + kRoundWords - 1) / kRoundWords;
+    const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(need, static_cast<size_t>(per_sm) * sms)));
+    long long *d_done = nullptr;
+    Workspace ws(s);
+    const size_t o_done = ws.reserve<long long>(1);
+    int rc = ws.commit();
+    if (rc) return rc;
+    d_done = ws.at<long long>(o_done);
+    LoopArgs<T> a{f, fh, codes, cnt, hp, req, act[0], act[1], slots, first, max_sweeps, d_done, g, eps, delta, q};
+    void *args[] = {&a};
+    if (et) PMSZ_CUDA(cudaEventRecord(et->ev[0], s));
+    PMSZ_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k_sweep_loop<T>), dim3(grid), dim3(kListBlock),
+                                          args, 0, s));
+    if (et) PMSZ_CUDA(cudaEventRecord(et->ev[1], s));
+    long long h = 0;
+    PMSZ_CUDA(cudaMemcpyAsync(&h, d_done, sizeof(h), cudaMemcpyDeviceToHost, s));
+    PMSZ_CUDA(cudaStreamSynchronize(s));
+    if (et) {
+        float ms = 0;
+        PMSZ_CUDA(cudaEventElapsedTime(&ms, et->ev[0], et->ev[1]));
+        *ms_acc += ms;
+    }
+    *done = h;
+    return ws.release();
+}
+
+// Grid of the list-compaction kernels: one block per 2048-word round, at most
+// 16 blocks per SM (grid-stride beyond).
+static inline unsigned list_grid(const Geom &g) {
+    const size_t want = (g.nwords + kRoundWords - 1) / kRoundWords;
+    return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(want, 152 * 16)));
+}
+
 int check_geom(size_t nx, size_t ny, size_t nz) {
     if (nx == 0 || ny == 0 || nz == 0) return set_error(PMSZ_ERR_ARG, "field dimensions must be positive");
     if (nx > (1u << 30) || ny > 65535 * 8 || nz > 65535)
         return set_error(PMSZ_ERR_ARG, "field dimensions exceed the supported range (nz <= 65535)");
+    if (((nx + 31) / 32) * ny * nz >= (static_cast<size_t>(1) << 32))
+        return set_error(PMSZ_ERR_ARG, "field too large: ceil(nx/32)*ny*nz must stay below 2^32");
     return PMSZ_OK;
 }
 
@@ -310,7 +364,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const size_t o_a0 = ws.reserve<uint32_t>(g.nwords);
     const size_t o_a1 = ws.reserve<uint32_t>(g.nwords);
     const size_t o_slots = ws.reserve<SweepSlot>(static_cast<size_t>(max_sweeps));
+    const size_t o_hp = ws.reserve<uint32_t>(g.n);
     if ((rc = ws.commit())) return rc;
+    uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
     uint8_t *cnt = ws.at<uint8_t>(o_cnt);
     uint32_t *req = ws.at<uint32_t>(o_req);
@@ -342,14 +398,14 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         uint32_t *a_next = act[cur ^ 1];
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
         if (sweeps == 0) {
-            k_detect_full<T, true><<<grid3(g), blk3, 0, s>>>(f, fh, codes, req, a_next, slot, g);
+            k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g);
         } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
-            k_detect_full<T, false><<<grid3(g), blk3, 0, s>>>(nullptr, fh, codes, req, a_next, slot, g);
+            k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g);
         } else {
-            k_detect_sparse<T><<<stride_grid(g.nwords), 256, 0, s>>>(fh, codes, act[cur], a_next, req, slot, g);
+            k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
-        k_apply<T><<<stride_grid(g.nwords), 256, 0, s>>>(f, fh, cnt, req, a_next, slot, g, eps, delta, q);
+        k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[2], s));
         launches += 2;
         PMSZ_CUDA(cudaGetLastError());
@@ -376,6 +432,33 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             break;
         }
         cur ^= 1;
+        // Once the next active set is small, per-sweep launches and host round
+        // trips dominate: hand the remaining sweeps to one cooperative launch.
+        const unsigned long long est_next = 15ull * h.changed + h.fdir;
+        if (!(flags & PMSZ_FLAG_FULL_SWEEPS) && sweeps < max_sweeps &&
+            est_next <= std::max<unsigned long long>(g.n / 32, 1ull << 16)) {
+            int64_t done = 0;
+            if ((rc = run_sweep_loop<T>(f, fh, codes, cnt, hp, req, act, slots, sweeps, max_sweeps, g, eps, delta, q,
+                                        s, timing ? &et : nullptr, &ms_detect, &done)))
+                return rc;
+            ++launches;
+            const size_t m = static_cast<size_t>(done - sweeps);
+            if (m) {
+                std::vector<SweepSlot> tail(m);
+                PMSZ_CUDA(cudaMemcpyAsync(tail.data(), slots + sweeps, m * sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
+                PMSZ_CUDA(cudaStreamSynchronize(s));
+                for (const SweepSlot &t : tail) {
+                    log.push_back(t);
+                    edits += t.requested;
+                }
+                const SweepSlot &last = tail.back();
+                if (last.fmax == 0 && last.fmin == 0 && last.fdir == 0) status = PMSZ_OK;
+                else if (last.progressed == 0)
+                    set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
+            }
+            sweeps = done;
+            break;
+        }
     }
     float ms_total = 0;
     PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
@@ -408,7 +491,7 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
     int rc = check_geom(nx, ny, nz);
     if (rc) return rc;
     const Geom g = make_geom(nx, ny, nz);
-    k_codes<T><<<grid3(g), dim3(32, 8, 1), 0, s>>>(v, codes, g);
+    k_tiled<T, kCodes><<<tiled_grid(g), dim3(kTX, kTY, 1), 0, s>>>(v, nullptr, codes, nullptr, nullptr, nullptr, nullptr, g);
     PMSZ_CUDA(cudaGetLastError());
     return PMSZ_OK;
 }

@@ -1,0 +1,533 @@
+// tiled.cuh -- proxy-based sweep kernels, included by correct.cu after its
+// shared device helpers.
+//
+// GB300 executes integer compare / min / max (and FP32 min / max) on one
+// 64-lane-per-clock pipe per SM, so a 15-point argmax / argmin on 64-bit keys
+// (about five instructions per candidate) is what bounds the sweep, not HBM.
+// These kernels compare 32-bit PROXIES instead:
+//
+//   proxy(v) = high 32 bits of the order-preserving key, low 4 bits cleared
+//
+// so that `proxy + rank` packs a candidate's stencil rank into the free bits
+// and a whole argmax is one min/max instruction per candidate.  Truncation
+// can only merge keys, never reorder them (key_a < key_b => proxy_a <=
+// proxy_b), so the packed chain is exact whenever the winning proxy is
+// unique.  A second chain with the ranks reversed (15 - r) picks the LOWEST
+// rank among tied proxies; both chains agree exactly when the winner is
+// unique -- the exactness certificate.  Where they disagree (ties in the
+// truncated proxy) the voxel takes the exact path on full keys.
+//
+// Out-of-domain stencil cells hold proxy 0: as `0 + r` they lose every max
+// chain (real proxies are >= 16), and the min chains add -16 (or -1) so that
+// they wrap to the top of the range and lose every min chain; no per-lane
+// boundary branch is needed on the fast path.
+#pragma once
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
+
+namespace pmsz {
+
+__device__ __forceinline__ uint32_t proxy_of_key(uint64_t k) { return static_cast<uint32_t>(k >> 32) & ~15u; }
+__device__ __forceinline__ uint32_t proxy_of_key(uint32_t k) { return k & ~15u; }
+template <typename T>
+__device__ __forceinline__ uint32_t proxy_of(T v) { return proxy_of_key(okey(v)); }
+
+struct Ext {
+    int asc, desc;
+    bool exact;
+};
+
+// Packed argmax / argmin of 15 proxies in rank order, with certificates.
+// General form: out-of-domain candidates carry proxy 0; the min chains add
+// -16 (and -1) so those wrap to the top of the range and lose.
+__device__ __forceinline__ Ext proxy_ext(const uint32_t (&t)[15]) {
+    uint32_t M = t[0], M2 = t[0] + 15u, m = t[0] - 16u, m2 = t[0] - 1u;
+#pragma unroll
+    for (int r = 1; r < 15; ++r) {
+        M = max(M, t[r] + static_cast<uint32_t>(r));
+        M2 = max(M2, t[r] + static_cast<uint32_t>(15 - r));
+        m = min(m, t[r] + (static_cast<uint32_t>(r) - 16u));
+        m2 = min(m2, t[r] + (0u - 1u - static_cast<uint32_t>(r)));
+    }
+    Ext e;
+    e.asc = static_cast<int>(M & 15u);
+    e.desc = static_cast<int>(m & 15u);
+    e.exact = e.asc == 15 - static_cast<int>(M2 & 15u) && e.desc == 15 - static_cast<int>(m2 & 15u);
+    return e;
+}
+
+// Interior form (all 15 candidates inside the domain): the max and min chains
+// share the packed values t + r and t + (15 - r), half the adds.
+__device__ __forceinline__ Ext proxy_ext_interior(const uint32_t (&t)[15]) {
+    uint32_t M = t[0], m = t[0], M2 = t[0] + 15u, m2 = M2;
+#pragma unroll
+    for (int r = 1; r < 15; ++r) {
+        const uint32_t a = t[r] + static_cast<uint32_t>(r), b = t[r] + static_cast<uint32_t>(15 - r);
+        M = max(M, a);
+        m = min(m, a);
+        M2 = max(M2, b);
+        m2 = min(m2, b);
+    }
+    Ext e;
+    e.asc = static_cast<int>(M & 15u);
+    e.desc = static_cast<int>(m & 15u);
+    e.exact = e.asc == 15 - static_cast<int>(M2 & 15u) && e.desc == 15 - static_cast<int>(m2 & 15u);
+    return e;
+}
+
+constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kRing = 4, kZChunk = 32;
+constexpr int kCells = kHX * kHY, kThreads = kTX * kTY;
+enum TileMode { kFirst = 0, kDetect = 1, kCodes = 2 };
+
+template <typename T, int NF>
+struct TileSmem {
+    uint32_t p[NF][kRing][kHY][kHX];                  // proxies
+    typename KeyOf<T>::type k[NF][kRing][kHY][kHX];   // full keys, for the rare exact path
+};
+
+__host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; }
+
+// ---------------------------------------------------------------------------
+// Tiled full-field pass.  Block (32, 8) owns a 32x8 column of the field and
+// marches it through kZChunk planes; planes (with a one-voxel halo) stream
+// through a 4-slot ring in shared memory, prefetched two planes ahead, one
+// barrier per plane.  Each thread loads the same (at most two) cells of every
+// plane, so their coordinates are decoded once per block.
+//   kFirst : fa = f, fb = fhat.  Labels f (code byte), writes the proxy array
+//            of fhat, and runs the first detection (iscriticle data_type=1
+//            fused with the first data_type=0 pass).
+//   kDetect: fa = fhat; the original codes come from `codes` (full sweep).
+//   kCodes : fa = a field; writes its code byte only (pmsz_codes_*).
+// ---------------------------------------------------------------------------
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
+                                                    uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
+                                                    uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                    SweepSlot *slot, Geom g) {
+    constexpr int NF = MODE == kFirst ? 2 : 1;
+    using K = typename KeyOf<T>::type;
+    __shared__ TileSmem<T, NF> sm;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
+    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
+    const int zb = blockIdx.z * kZChunk, ze = min(g.nz, zb + kZChunk);
+    const int x = x0 + tx, y = y0 + ty;
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+
+    // this thread's load cells (tid and tid + 256 of the 34 x 10 halo plane)
+    int cell_s[2];
+    size_t cell_g[2];
+    bool cell_in[2], cell_own[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * kThreads;
+        const int cy = c / kHX, cx = c - cy * kHX;
+        const int gx = x0 - 1 + cx, gy = y0 - 1 + cy;
+        cell_s[j] = c;
+        cell_in[j] = c < kCells && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+        cell_own[j] = cell_in[j] && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY;
+        cell_g[j] = cell_in[j] ? static_cast<size_t>(gx) + static_cast<size_t>(gy) * g.nx : 0;
+    }
+    uint32_t bad = 0;
+
+    auto load_plane = [&](int zz) {
+        const int s = zz & (kRing - 1);
+        const bool zin = zz >= 0 && zz < g.nz;
+        const bool zown = zz >= zb && zz < ze;
+        const size_t zoff = zin ? static_cast<size_t>(zz) * plane : 0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (cell_s[j] >= kCells) continue;
+            const bool in = cell_in[j] && zin;
+#pragma unroll
+            for (int F = 0; F < NF; ++F) {
+                K key = 0;
+                uint32_t px = 0;
+                if (in) {
+                    const T v = (F == 0 ? fa : fb)[zoff + cell_g[j]];
+                    key = okey(v);
+                    px = proxy_of_key(key);
+                    if (MODE == kFirst && cell_own[j] && zown) {
+                        bad |= bad_value(v) ? 1u : 0u;
+                        if (F == 1) hp[zoff + cell_g[j]] = px;
+                    }
+                }
+                (&sm.p[F][s][0][0])[cell_s[j]] = px;
+                (&sm.k[F][s][0][0])[cell_s[j]] = key;
+            }
+        }
+    };
+
+    auto ext = [&](int F, int z, const int (&slots)[3], bool interior) -> Ext {
+        uint32_t t[15];
+#pragma unroll
+        for (int r = 0; r < 15; ++r) t[r] = sm.p[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+        Ext e = interior ? proxy_ext_interior(t) : proxy_ext(t);
+        if (!e.exact) {  // ties in the truncated proxies: exact keys
+            K k[15];
+#pragma unroll
+            for (int r = 0; r < 15; ++r) k[r] = sm.k[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+            arg_ext(k, valid_mask(x, y, z, g.nx, g.ny, g.nz), e.asc, e.desc);
+        }
+        return e;
+    };
+
+    load_plane(zb - 1);
+    load_plane(zb);
+    if (zb + 1 <= ze) load_plane(zb + 1);
+    __syncthreads();
+    uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
+    const bool in = x < g.nx && y < g.ny;
+    const bool xy_interior = x0 >= 1 && x0 + kTX <= g.nx - 1 && y >= 1 && y <= g.ny - 2;  // warp-uniform
+    for (int z = zb; z < ze; ++z) {
+        if (z + 2 <= ze) load_plane(z + 2);
+        const int slots[3] = {(z + kRing - 1) & (kRing - 1), z & (kRing - 1), (z + 1) & (kRing - 1)};
+        const bool interior = xy_interior && z >= 1 && z <= g.nz - 2;
+        uint32_t tm = 0;
+        if (in) {
+            const size_t i = flat(g, x, y, z);
+            if (MODE == kCodes) {
+                const Ext e = ext(0, z, slots, interior);
+                codes[i] = static_cast<uint8_t>(e.asc | (e.desc << 4));
+            } else {
+                int oasc, odesc;
+                Ext e;
+                if (MODE == kFirst) {
+                    const Ext o = ext(0, z, slots, interior);
+                    oasc = o.asc;
+                    odesc = o.desc;
+                    codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
+                    e = ext(1, z, slots, interior);
+                } else {
+                    const uint8_t c = codes[i];
+                    oasc = c & 15;
+                    odesc = c >> 4;
+                    e = ext(0, z, slots, interior);
+                }
+                tm = detect_rules(e.asc, e.desc, oasc, odesc, cmax, cmin, cdir);
+                if (tm) request_targets(req, g, x, y, z, tm);
+                ++active;
+            }
+        }
+        if (MODE != kCodes) {
+            const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
+            if (tx == 0 && y < g.ny && mism) act_next[word_of(g, x0, y, z)] = mism;
+        }
+        __syncthreads();
+    }
+    if (MODE != kCodes) flush_counts(slot, cmax, cmin, cdir, active, bad);
+}
+
+// ---------------------------------------------------------------------------
+// Load policies.  Standalone sweep kernels read arrays that no thread of the
+// same launch writes through the read-only path (__ldg).  The persistent loop
+// kernel writes those arrays in one phase and reads them in the next, across
+// grid-wide barriers, so it reads them at L2 (__ldcg), never from a
+// possibly stale L1 line.
+// ---------------------------------------------------------------------------
+struct LdgLoads {
+    template <class P>
+    static __device__ __forceinline__ P ld(const P *p) { return __ldg(p); }
+};
+struct CgLoads {
+    template <class P>
+    static __device__ __forceinline__ P ld(const P *p) { return __ldcg(p); }
+};
+
+// ---------------------------------------------------------------------------
+// Block-local compaction of a bitmap.  A round covers 2048 consecutive words:
+// each of the 256 threads loads 8 of them with two 16-byte loads, and one
+// barrier skips the round when all are empty (late sweeps touch a few words of
+// a large bitmap, so the scan must move as much per barrier as it can).  In a
+// non-empty round the set bits of all 2048 words are ranked by a block scan
+// and written to a dense work list in shared memory (entries (word << 5) |
+// bit, word local to the round), in passes of at most kListCap entries, and
+// all 256 threads share the list: a sparse or clustered bitmap still keeps
+// every lane busy, and a sparse round costs a handful of barriers.
+// ---------------------------------------------------------------------------
+constexpr int kListBlock = 256;
+constexpr int kWordsPerThread = 8;
+constexpr int kRoundWords = kListBlock * kWordsPerThread;
+constexpr uint32_t kListCap = 8192;
+
+struct ListSmem {
+    uint32_t list[kListCap];
+    uint32_t mask[kRoundWords];   // per-word result bits (mismatch / changed)
+    uint32_t warp_tot[kListBlock / 32];
+    uint32_t total;
+};
+
+// Loads the 8 words of this thread for the round starting at `base` (bitmaps
+// are 256-byte aligned and rounds start at multiples of 2048 words, so the
+// vector loads are aligned); returns whether any word of the block is set.
+template <class L>
+__device__ __forceinline__ bool load_round(const uint32_t *__restrict__ bm, size_t base, const Geom &g,
+                                           uint32_t (&w8)[kWordsPerThread]) {
+    const size_t w0 = base + static_cast<size_t>(threadIdx.x) * kWordsPerThread;
+    if (w0 + kWordsPerThread <= g.nwords) {
+        const uint4 a = L::ld(reinterpret_cast<const uint4 *>(bm + w0));
+        const uint4 b = L::ld(reinterpret_cast<const uint4 *>(bm + w0 + 4));
+        w8[0] = a.x; w8[1] = a.y; w8[2] = a.z; w8[3] = a.w;
+        w8[4] = b.x; w8[5] = b.y; w8[6] = b.z; w8[7] = b.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < kWordsPerThread; ++j) w8[j] = w0 + j < g.nwords ? L::ld(bm + w0 + j) : 0u;
+    }
+    uint32_t any = 0;
+#pragma unroll
+    for (int j = 0; j < kWordsPerThread; ++j) any |= w8[j];
+    return __syncthreads_or(any != 0) != 0;
+}
+
+// Calls work(x, y, z, word_local) for every set bit of bitmap `bm` (clearing
+// the bitmap); a true result sets the voxel's bit in a per-word result mask,
+// and flush(w, mask) is then called once per word with a non-zero mask, by the
+// thread that owns the word.  Every thread of the block must call this.
+template <class L, class Work, class Flush>
+__device__ __forceinline__ void for_each_set_bit(ListSmem &sm, uint32_t *__restrict__ bm, const Geom &g, Work work,
+                                                 Flush flush) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (size_t base = static_cast<size_t>(blockIdx.x) * kRoundWords; base < g.nwords;
+         base += static_cast<size_t>(gridDim.x) * kRoundWords) {
+        uint32_t w8[kWordsPerThread];
+        if (!load_round<L>(bm, base, g, w8)) continue;  // uniform
+        const size_t w0 = base + static_cast<size_t>(t) * kWordsPerThread;
+        uint32_t c = 0;
+#pragma unroll
+        for (int j = 0; j < kWordsPerThread; ++j) {
+            if (w8[j]) bm[w0 + j] = 0;
+            sm.mask[t * kWordsPerThread + j] = 0;
+            c += __popc(w8[j]);
+        }
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) sm.warp_tot[warp] = inc;
+        __syncthreads();
+        if (t == 0) {
+            uint32_t run = 0;
+            for (int k = 0; k < kListBlock / 32; ++k) {
+                const uint32_t v = sm.warp_tot[k];
+                sm.warp_tot[k] = run;
+                run += v;
+            }
+            sm.total = run;
+        }
+        __syncthreads();
+        const uint32_t first = sm.warp_tot[warp] + inc - c, total = sm.total;
+        for (uint32_t lo = 0; lo < total; lo += kListCap) {
+            const uint32_t hi = lo + kListCap;
+            if (first < hi && first + c > lo) {  // some of my entries fall in this pass
+                uint32_t rank = first;
+#pragma unroll
+                for (int j = 0; j < kWordsPerThread; ++j) {
+                    uint32_t bits = w8[j];
+                    while (bits) {
+                        const int b = __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        if (rank >= lo && rank < hi)
+                            sm.list[rank - lo] = (static_cast<uint32_t>(t * kWordsPerThread + j) << 5) | static_cast<uint32_t>(b);
+                        ++rank;
+                    }
+                }
+            }
+            __syncthreads();
+            const uint32_t n = min(kListCap, total - lo);
+            for (uint32_t k = t; k < n; k += kListBlock) {
+                const uint32_t e = sm.list[k];
+                const uint32_t wl = e >> 5;
+                const int b = static_cast<int>(e & 31u);
+                int wx, y, z;
+                word_coords(g, base + wl, wx, y, z);
+                if (work(wx * 32 + b, y, z, wl)) atomicOr(&sm.mask[wl], 1u << b);
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int j = 0; j < kWordsPerThread; ++j) {
+            const uint32_t m = sm.mask[t * kWordsPerThread + j];
+            if (w8[j] && m) flush(w0 + j, m);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sparse detection over the active bitmap, reading the proxy array of fhat.
+// Mismatching voxels are collected per word and written to act_next by the
+// word's owner thread (one writer per word).
+// ---------------------------------------------------------------------------
+template <class L, typename T>
+__device__ __forceinline__ void sparse_detect_body(ListSmem &sm, const T *__restrict__ fh, const uint32_t *__restrict__ hp,
+                                                   const uint8_t *__restrict__ codes, uint32_t *__restrict__ act_cur,
+                                                   uint32_t *__restrict__ act_next, uint32_t *__restrict__ req,
+                                                   SweepSlot *slot, const Geom &g) {
+    const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
+    uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
+    auto work = [&](int x, int y, int z, uint32_t) -> bool {
+        const size_t i = flat(g, x, y, z);
+        const bool interior = x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
+        const uint32_t valid = interior ? kAllValid : valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        const uint32_t *c0 = hp + i;
+        uint32_t t[15];
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+            t[r] = ((valid >> r) & 1u) ? L::ld(c0 + off) : 0u;
+        }
+        Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
+        if (!ex.exact) {
+            typename KeyOf<T>::type kk[15];
+#pragma unroll
+            for (int r = 0; r < 15; ++r) {
+                const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+                kk[r] = ((valid >> r) & 1u) ? okey(L::ld(fh + (static_cast<ptrdiff_t>(i) + off)))
+                                            : typename KeyOf<T>::type(0);
+            }
+            arg_ext(kk, valid, ex.asc, ex.desc);
+        }
+        const uint8_t c = __ldg(codes + i);
+        const uint32_t tm = detect_rules(ex.asc, ex.desc, c & 15, c >> 4, cmax, cmin, cdir);
+        ++active;
+        if (tm) request_targets(req, g, x, y, z, tm);
+        return tm != 0;
+    };
+    auto flush = [&](size_t w, uint32_t m) { act_next[w] = m; };
+    for_each_set_bit<L>(sm, act_cur, g, work, flush);
+    flush_counts(slot, cmax, cmin, cdir, active, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Apply with the proxy array: applyDeltaBuffer_local (pMSz.cu:623-645) on
+// every requested vertex, in T:
+//   if |f - (fhat - delta)| <= eps && cnt < q-1 { fhat -= delta; cnt++ }
+//   else { cnt = q; fhat = f - eps }
+// the proxy of every changed value refreshed, and the closed stencil of the
+// changed vertices (collected per word) marked in act_next by the word's
+// owner thread.
+// ---------------------------------------------------------------------------
+template <class L, typename T>
+__device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f, T *__restrict__ fh,
+                                           uint8_t *__restrict__ cnt, uint32_t *__restrict__ hp,
+                                           uint32_t *__restrict__ req, uint32_t *__restrict__ act_next, SweepSlot *slot,
+                                           const Geom &g, T eps, T delta, int q) {
+    uint32_t nreq = 0, nchg = 0, nprog = 0;
+    auto work = [&](int x, int y, int z, uint32_t) -> bool {
+        const size_t v = flat(g, x, y, z);
+        const T old = L::ld(fh + v);
+        const uint8_t oc = L::ld(cnt + v);
+        const T fv = __ldg(f + v);
+        const T lowered = old - delta;
+        T nv;
+        uint8_t nc;
+        if (fabs(fv - lowered) <= eps && static_cast<int>(oc) < q - 1) {
+            nv = lowered;
+            nc = static_cast<uint8_t>(oc + 1);
+        } else {
+            nc = static_cast<uint8_t>(q);
+            nv = fv - eps;
+        }
+        fh[v] = nv;
+        cnt[v] = nc;
+        const bool chg = bits_of(old) != bits_of(nv);
+        if (chg) hp[v] = proxy_of(nv);
+        ++nreq;
+        nprog += (chg || nc != oc) ? 1u : 0u;
+        return chg;
+    };
+    auto flush = [&](size_t w, uint32_t m) {
+        nchg += __popc(m);
+        int wx, y, z;
+        word_coords(g, w, wx, y, z);
+        mark_stencil(act_next, g, wx, y, z, m);
+    };
+    for_each_set_bit<L>(sm, req, g, work, flush);
+    nreq = warp_sum_u32(nreq);
+    nchg = warp_sum_u32(nchg);
+    nprog = warp_sum_u32(nprog);
+    if ((threadIdx.x & 31) == 0) {
+        if (nreq) atomicAdd(&slot->requested, (unsigned long long)nreq);
+        if (nchg) atomicAdd(&slot->changed, (unsigned long long)nchg);
+        if (nprog) atomicAdd(&slot->progressed, (unsigned long long)nprog);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kListBlock, 3) k_sparse_px(const T *__restrict__ fh, const uint32_t *__restrict__ hp,
+                                                          const uint8_t *__restrict__ codes, uint32_t *__restrict__ act_cur,
+                                                          uint32_t *__restrict__ act_next, uint32_t *__restrict__ req,
+                                                          SweepSlot *slot, Geom g) {
+    __shared__ ListSmem sm;
+    sparse_detect_body<LdgLoads>(sm, fh, hp, codes, act_cur, act_next, req, slot, g);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kListBlock) k_apply_px(const T *__restrict__ f, T *__restrict__ fh,
+                                                         uint8_t *__restrict__ cnt, uint32_t *__restrict__ hp,
+                                                         uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                         SweepSlot *slot, Geom g, T eps, T delta, int q) {
+    __shared__ ListSmem sm;
+    apply_body<LdgLoads>(sm, f, fh, cnt, hp, req, act_next, slot, g, eps, delta, q);
+}
+
+// Stop rule of the correction loop after a sweep (the slot of that sweep):
+// converged (no mismatch), stuck (nothing could change), or out of sweeps.
+__host__ __device__ __forceinline__ bool sweep_stops(unsigned long long fmax, unsigned long long fmin,
+                                                     unsigned long long fdir, unsigned long long progressed,
+                                                     int64_t sweeps_done, int64_t max_sweeps) {
+    return (fmax == 0 && fmin == 0 && fdir == 0) || progressed == 0 || sweeps_done >= max_sweeps;
+}
+
+template <typename T>
+struct LoopArgs {
+    const T *f;
+    T *fh;
+    const uint8_t *codes;
+    uint8_t *cnt;
+    uint32_t *hp, *req, *act0, *act1;
+    SweepSlot *slots;
+    int64_t first;       // index of the first sweep this launch runs
+    int64_t max_sweeps;
+    long long *sweeps_out;
+    Geom g;
+    T eps, delta;
+    int q;
+};
+
+// ---------------------------------------------------------------------------
+// The remaining sweeps of the loop in one cooperative launch: detect, grid
+// barrier, apply, grid barrier, then every thread reads the sweep's counters
+// and takes the same stop decision, so all blocks leave together.  Sweep k
+// reads act[k & 1] and fills act[(k + 1) & 1].  The loop is bounded by
+// max_sweeps.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kListBlock, 2) k_sweep_loop(LoopArgs<T> a) {
+    __shared__ ListSmem sm;
+    cg::grid_group grid = cg::this_grid();
+    int64_t k = a.first;
+    while (true) {
+        const SweepSlot *p = a.slots + (k - 1);
+        if (sweep_stops(__ldcg(&p->fmax), __ldcg(&p->fmin), __ldcg(&p->fdir), __ldcg(&p->progressed), k,
+                        a.max_sweeps))
+            break;
+        uint32_t *cur = (k & 1) ? a.act1 : a.act0;
+        uint32_t *nxt = (k & 1) ? a.act0 : a.act1;
+        sparse_detect_body<CgLoads>(sm, a.fh, a.hp, a.codes, cur, nxt, a.req, a.slots + k, a.g);
+        grid.sync();
+        apply_body<CgLoads>(sm, a.f, a.fh, a.cnt, a.hp, a.req, nxt, a.slots + k, a.g, a.eps, a.delta, a.q);
+        grid.sync();
+        ++k;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.sweeps_out = k;
+}
+
+inline dim3 tiled_grid(const Geom &g) {
+    return dim3(static_cast<unsigned>(g.wpr), static_cast<unsigned>((g.ny + kTY - 1) / kTY),
+                static_cast<unsigned>((g.nz + kZChunk - 1) / kZChunk));
+}
+
+}  // namespace pmsz
