@@ -59,6 +59,12 @@ def parse():
     p.add_argument("--cpu-slices", type=int, default=64, help="z-slices of the CPU sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--workload", choices=["plain", "batch", "serve"], default="plain",
+                   help="plain: one 512^3 field (the headline); batch: 64 mixed fp32 fields; "
+                        "serve: Poisson job stream through the correction server")
+    p.add_argument("--serve-jobs", type=int, default=120)
+    p.add_argument("--serve-rates", default="100,300,1000,3000", help="arrival rates (jobs/s) to sweep")
+    p.add_argument("--batch-fields", type=int, default=64)
     return p.parse_args()
 
 
@@ -315,10 +321,166 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
 
 
+def batch_specs(count: int, base_seed: int = 100):
+    """64 fp32 Perlin fields, seeds 100..163: each axis uniform in 32..256, eps
+    log-uniform in [1e-5, 1e-2] of the [0,1] range, first half sz3, second
+    half zfp stand-ins."""
+    specs = []
+    for k in range(count):
+        rs = np.random.RandomState(base_seed + k)
+        shape = tuple(int(v) for v in rs.randint(32, 257, size=3))
+        eb = float(10 ** rs.uniform(-5, -2))
+        comp = "sz3" if k < count // 2 else "zfp"
+        specs.append((base_seed + k, shape, eb, comp))
+    return specs
+
+
+def run_batch(args):
+    """Batched form: all fields in one pmsz_correct_batch call vs the same
+    fields corrected one by one with pmsz_correct_f32."""
+    import torch
+    from pmsz_anonymous_gb300 import _build, api
+    _build.build()
+    dev = torch.device("cuda", 0)
+    specs = batch_specs(args.batch_fields)
+    fields = []
+    for seed, shape, eb, comp in specs:
+        f = api.gen_perlin(shape, seed, 4, 1 / 32, dtype=torch.float32, device=dev)
+        fields.append((f, api.standin(f, eb, comp, seed), eb))
+    torch.cuda.synchronize()
+    nvox = sum(f.numel() for f, _, _ in fields)
+    work = [fh.clone() for _, fh, _ in fields]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def refresh():
+        for w, (_, fh, _) in zip(work, fields):
+            w.copy_(fh)
+
+    def one_by_one():
+        for w, (f, _, eb) in zip(work, fields):
+            api.correct(f, w, eb)
+
+    def batched():
+        api.correct_batch([(f, w, eb) for w, (f, _, eb) in zip(work, fields)])
+
+    times = {}
+    for name, fn in (("plain", one_by_one), ("batch", batched)):
+        for _ in range(args.warmup):
+            refresh()
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            refresh()
+            torch.cuda.synchronize()
+            start.record()
+            fn()
+            stop.record()
+            stop.synchronize()
+            ts.append(start.elapsed_time(stop))
+        times[name] = statistics.mean(ts)
+    refresh()
+    res = api.correct_batch([(f, w, eb) for w, (f, _, eb) in zip(work, fields)])
+    out = {
+        "metric": "batched vox/s (64 mixed fp32 fields, one pmsz_correct_batch call)",
+        "value": nvox / (times["batch"] * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": times["batch"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(specs)} fp32 Perlin fBm fields (seeds {specs[0][0]}-{specs[-1][0]}, 4 octaves, "
+                               "base 1/32), axes uniform 32-256, eps log-uniform [1e-5,1e-2], half sz3 / half zfp "
+                               "stand-ins", "voxels": nvox, "fields": len(specs)},
+        "plain_one_by_one": {"value": nvox / (times["plain"] * 1e-3) / 1e9, "unit": "Gvox/s",
+                             "ms_per_step": times["plain"]},
+        "batch_over_plain": times["plain"] / times["batch"],
+        "statuses": sorted(set(r.status for r in res)),
+        "sweeps_max": max(r.sweeps for r in res),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def serve_specs(count: int, base_seed: int = 1000):
+    """Served stream: per-job seed base+id, 3-6 octaves, each axis log-uniform
+    in 32..384, 70% fp32 / 30% fp64, eps log-uniform in [1e-5, 1e-2], sz3 /
+    zfp stand-ins 50/50."""
+    out = []
+    for j in range(count):
+        rs = np.random.RandomState(base_seed + j)
+        shape = tuple(int(round(np.exp(rs.uniform(np.log(32), np.log(384))))) for _ in range(3))
+        out.append({"seed": base_seed + j, "shape": shape, "octaves": int(rs.randint(3, 7)),
+                    "f64": bool(rs.uniform() < 0.3), "eb": float(10 ** rs.uniform(-5, -2)),
+                    "comp": "sz3" if rs.uniform() < 0.5 else "zfp"})
+    return out
+
+
+def run_serve(args):
+    """Continuous-batching server under Poisson arrivals at swept rates."""
+    import threading
+    import torch
+    from pmsz_anonymous_gb300 import _build, api
+    _build.build()
+    dev = torch.device("cuda", 0)
+    specs = serve_specs(args.serve_jobs)
+    jobs = []
+    for sp in specs:
+        dt = torch.float64 if sp["f64"] else torch.float32
+        f = api.gen_perlin(sp["shape"], sp["seed"], sp["octaves"], 1 / 32, dtype=dt, device=dev)
+        jobs.append((f, api.standin(f, sp["eb"], sp["comp"], sp["seed"]), sp["eb"]))
+    work = [fh.clone() for _, fh, _ in jobs]
+    torch.cuda.synchronize()
+    nvox = sum(f.numel() for f, _, _ in jobs)
+    rows = []
+    rng = np.random.RandomState(7)
+    for rate in [float(r) for r in args.serve_rates.split(",")]:
+        for w, (_, fh, _) in zip(work, jobs):
+            w.copy_(fh)
+        torch.cuda.synchronize()
+        gaps = rng.exponential(1.0 / rate, size=len(jobs))
+        infos = [None] * len(jobs)
+        with api.Server(hbm_budget_bytes=120 * 10**9) as srv:
+            ids = [None] * len(jobs)
+            done = threading.Event()
+
+            def waiter():
+                for k in range(len(jobs)):
+                    while ids[k] is None:
+                        time.sleep(0.0002)
+                    infos[k] = srv.wait(ids[k])
+                done.set()
+
+            th = threading.Thread(target=waiter)
+            th.start()
+            t0 = time.perf_counter()
+            due = t0
+            for k, ((f, _, eb), w) in enumerate(zip(jobs, work)):
+                due += gaps[k]
+                while time.perf_counter() < due:
+                    pass
+                ids[k] = srv.submit(f, w, eb)
+            done.wait()
+            wall = time.perf_counter() - t0
+            th.join()
+        lat = np.array([i["latency_ms"] for i in infos])
+        rows.append({"rate_jobs_s": rate, "jobs_s": len(jobs) / wall, "gvox_s": nvox / wall / 1e9,
+                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "queue_p99_ms": float(np.percentile([i["queue_ms"] for i in infos], 99)),
+                     "ok": int(sum(i["status"] == 0 for i in infos))})
+    best = max(rows, key=lambda r: r["jobs_s"])
+    print(json.dumps({
+        "metric": "served correction stream: jobs/s and p50/p99 latency", "value": best["jobs_s"], "unit": "jobs/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f32/f64", "data": "synthetic",
+        "config": {"workload": f"{len(jobs)} jobs, Poisson arrivals, axes log-uniform 32-384, 70% fp32 / 30% fp64, "
+                               "3-6 octaves, eps log-uniform [1e-5,1e-2], sz3/zfp stand-ins 50/50, 120 GB budget",
+                   "voxels": nvox},
+        "rates": rows}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -138,6 +138,76 @@ int pmsz_correct_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t
 int pmsz_correct_noalloc(const void *f, void *fhat, size_t elem_size, size_t nx, size_t ny, size_t nz,
                          double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
 
+/* One field of a batch: device pointers as for pmsz_correct_*, elem_size 4
+ * (float) or 8 (double). */
+typedef struct pmsz_field {
+    const void *f;
+    void *fhat;
+    size_t nx, ny, nz;
+    double eb;
+    uint32_t elem_size;
+    uint32_t reserved;
+} pmsz_field;
+
+/*
+ * pmsz_correct_batch: corrects `count` (1..4096) independent fields together --
+ * the batched form of the c_loops call (pMSz.cu:1872-2074), which the
+ * reference runs one field per program.  One fused first pass covers the tiles
+ * of every field, multi-field sweeps follow while the fields' active sets are
+ * large, and a single cooperative persistent launch finishes the light tail
+ * with a per-field stop decision on the device.  Every field keeps its own
+ * scratch, sweep index and stop state, so fields[i].fhat ends bit-identical to
+ * what pmsz_correct_* produces for that field alone, and results[i] /
+ * statuses[i] (either may be NULL) are what that call would report (timing
+ * fields 0).  Fields of both types may be mixed; they run as one batch per
+ * type.  Returns PMSZ_OK if every field converged, else the first non-OK
+ * status.
+ */
+int pmsz_correct_batch(const pmsz_field *fields, int count, const pmsz_opts *opts, pmsz_result *results,
+                       int *statuses, void *stream);
+
+/*
+ * Correction server (continuous batching).  The reference corrects one field
+ * per program run; the server accepts jobs from any host thread and runs them
+ * on the device current at pmsz_server_create.  A worker thread repeats
+ * generations: admit queued jobs in arrival order while the HBM budget (the
+ * job's two fields plus its scratch) and the running-job limit allow, run one
+ * sweep of every running job in shared multi-field launches (the fused first
+ * pass for jobs admitted now), and retire jobs whose correction stopped.  A
+ * job's result is bit-identical to pmsz_correct_* on the same field alone.
+ * Field pointers are device pointers the caller keeps alive, and whose
+ * producing work the caller has completed (e.g. synchronised) before submit;
+ * fhat is corrected in place.
+ */
+typedef struct pmsz_server pmsz_server;
+
+typedef struct pmsz_server_config {
+    size_t hbm_budget_bytes;  /* admission budget; 0 = unlimited */
+    int32_t max_jobs;         /* running jobs at once; <= 0 selects 256 (max 4096) */
+    int32_t q;                /* <= 0 selects 5 */
+    int64_t max_sweeps;       /* <= 0 selects 10000 */
+} pmsz_server_config;
+
+typedef struct pmsz_job_info {
+    int32_t done;             /* 1 once the job finished */
+    int32_t status;           /* PMSZ_* of the job's correction */
+    int64_t sweeps;
+    uint64_t edits;
+    double queue_ms;          /* submit -> admission */
+    double run_ms;            /* admission -> retirement */
+    double latency_ms;        /* submit -> retirement */
+} pmsz_job_info;
+
+int pmsz_server_create(const pmsz_server_config *cfg, pmsz_server **out);
+int pmsz_server_submit(pmsz_server *srv, const pmsz_field *field, uint64_t *job_id);
+/* Waits up to timeout_s seconds (< 0: forever, 0: poll) and fills *info;
+ * info->done tells whether the job finished. */
+int pmsz_server_wait(pmsz_server *srv, uint64_t job_id, double timeout_s, pmsz_job_info *info);
+/* Forgets a finished job. */
+int pmsz_server_release(pmsz_server *srv, uint64_t job_id);
+/* Finishes every submitted job, then stops the worker and frees the server. */
+int pmsz_server_destroy(pmsz_server *srv);
+
 /*
  * pmsz_codes_{f32,f64}: steepest-direction labelling of one field -- the
  * neighbour scan and or_types encoding of iscriticle data_type=1

@@ -225,3 +225,90 @@ def decode_clamps(blob: bytes, dtype) -> np.ndarray:
 
 def zstd_version() -> int:
     return int(capi.load().pmsz_zstd_version())
+
+
+def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None):
+    """Correct many fields together (pmsz_correct_batch).  items: sequence of
+    (f, fhat, eb) CUDA tensors / floats; each fhat is corrected in place.
+    Returns a list of CorrectResult, one per item."""
+    items = list(items)
+    n = len(items)
+    fields = (capi.Field * n)()
+    logs = [(capi.SweepRecord * int(max_sweeps))() for _ in range(n)]
+    results = (capi.Result * n)()
+    statuses = (ctypes.c_int * n)()
+    device = None
+    for k, (f, fh, eb) in enumerate(items):
+        _check_field(f, "f")
+        _check_field(fh, "fhat")
+        if f.shape != fh.shape or f.dtype != fh.dtype:
+            raise ValueError("f and fhat must share shape and dtype")
+        device = device or f.device
+        nx, ny, nz = _dims(f)
+        fields[k] = capi.Field(f.data_ptr(), fh.data_ptr(), nx, ny, nz, float(eb), f.element_size(), 0)
+        results[k].sweep_log = ctypes.cast(logs[k], ctypes.POINTER(capi.SweepRecord))
+        results[k].sweep_log_cap = int(max_sweeps)
+    opts = capi.Opts(int(q), 0, int(max_sweeps))
+    with torch.cuda.device(device):
+        st = capi.load().pmsz_correct_batch(fields, n, ctypes.byref(opts), results, statuses, _stream(stream))
+    if st not in (capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED, capi.PMSZ_ERR_ARG):
+        capi.check(st)
+    out = []
+    for k in range(n):
+        m = int(results[k].sweeps)
+        rows = np.array([[getattr(logs[k][i], key) for key in SWEEP_KEYS] for i in range(m)],
+                        dtype=np.uint64).reshape(m, len(SWEEP_KEYS))
+        out.append(CorrectResult(int(statuses[k]), m, int(results[k].iteration), int(results[k].edits), rows))
+    return out
+
+
+class Server:
+    """Continuous-batching correction server (pmsz_server_*).  submit() takes
+    (f, fhat, eb) CUDA tensors (fhat corrected in place; keep both alive until
+    the job finishes) and returns a job id; wait() returns a dict with the
+    job's status, sweeps, edits and queue / run / latency in ms."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_jobs: int = 256, q: int = 5, max_sweeps: int = 10000):
+        self._lib = capi.load()
+        cfg = capi.ServerConfig(int(hbm_budget_bytes), int(max_jobs), int(q), int(max_sweeps))
+        h = ctypes.c_void_p()
+        capi.check(self._lib.pmsz_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, f: torch.Tensor, fhat: torch.Tensor, eb: float) -> int:
+        _check_field(f, "f")
+        _check_field(fhat, "fhat")
+        nz, ny, nx = f.shape
+        fld = capi.Field(f.data_ptr(), fhat.data_ptr(), nx, ny, nz, float(eb), f.element_size(), 0)
+        jid = ctypes.c_uint64()
+        capi.check(self._lib.pmsz_server_submit(self._h, ctypes.byref(fld), ctypes.byref(jid)))
+        self._keep[jid.value] = (f, fhat)
+        return jid.value
+
+    def wait(self, job_id: int, timeout_s: float = -1.0) -> dict:
+        info = capi.JobInfo()
+        capi.check(self._lib.pmsz_server_wait(self._h, int(job_id), float(timeout_s), ctypes.byref(info)))
+        d = {k: getattr(info, k) for k, _ in capi.JobInfo._fields_}
+        if info.done:
+            self._keep.pop(job_id, None)
+            self._lib.pmsz_server_release(self._h, int(job_id))
+        return d
+
+    def close(self):
+        if self._h is not None:
+            capi.check(self._lib.pmsz_server_destroy(self._h))
+            self._h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -41,6 +41,20 @@ class VerifyResult(ctypes.Structure):
                 ("ds_mismatch", c_u64), ("bound_strict", c_u64), ("bound_beyond_clamp", c_u64)]
 
 
+class Field(ctypes.Structure):
+    _fields_ = [("f", c_void_p), ("fhat", c_void_p), ("nx", c_size), ("ny", c_size), ("nz", c_size),
+                ("eb", c_double), ("elem_size", c_u32), ("reserved", c_u32)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_size), ("max_jobs", c_i32), ("q", c_i32), ("max_sweeps", c_i64)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("done", c_i32), ("status", c_i32), ("sweeps", c_i64), ("edits", c_u64), ("queue_ms", c_double),
+                ("run_ms", c_double), ("latency_ms", c_double)]
+
+
 class HostOutputs(ctypes.Structure):
     _fields_ = [("deltas", c_void_p), ("clamp", c_void_p), ("n_clamp", c_u64), ("edit_count", c_u64),
                 ("verify", ctypes.POINTER(VerifyResult))]
@@ -72,6 +86,12 @@ SIGNATURES = {
     "pmsz_decode_clamps": (c_int, [_P, c_size, c_size, _P, _P]),
     "pmsz_free": (None, [_P]),
     "pmsz_zstd_version": (c_u32, []),
+    "pmsz_server_create": (c_int, [_P, _P]),
+    "pmsz_server_submit": (c_int, [_P, _P, _P]),
+    "pmsz_server_wait": (c_int, [_P, c_u64, c_double, _P]),
+    "pmsz_server_release": (c_int, [_P, c_u64]),
+    "pmsz_server_destroy": (c_int, [_P]),
+    "pmsz_correct_batch": (c_int, [_P, c_int, _P, _P, _P, _P]),
     "pmsz_correct_noalloc": (c_int, [_P, _P, c_size, c_size, c_size, c_size, c_double, _P, _P, _P]),
     "pmsz_correct_host_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
     "pmsz_correct_host_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),

@@ -1,0 +1,96 @@
+// batch.h -- multi-field correction: the per-field table the multi-field
+// kernels read, and the host driver shared by pmsz_correct_batch (batch.cu)
+// and the continuous-batching server (server.cpp).
+#pragma once
+#include "tiled.cuh"
+#include "internal.h"
+
+#include <string>
+#include <vector>
+
+namespace pmsz {
+
+constexpr int kMaxBatch = 4096;
+
+// One field of a multi-field run, as the kernels see it.
+template <typename T>
+struct Inst {
+    const T *f;
+    T *fh;
+    uint8_t *codes, *cnt;
+    uint32_t *hp, *req, *act0, *act1;
+    SweepSlot *slots;   // this field's slot of sweep k is slots[k * stride]
+    int64_t stride;
+    Geom g;
+    T eps, delta;
+    int q;
+    int64_t max_sweeps;
+    int64_t k;          // index of the field's next sweep
+    int active;         // runs sweeps
+    int first;          // joins now: its fused first pass runs in this generation
+    uint32_t tiles_x, tiles_y;
+};
+
+template <typename T>
+struct FieldSpec {
+    const T *f;
+    T *fh;
+    size_t nx, ny, nz;
+    double eb;
+};
+
+struct BatchOutcome {
+    int status = PMSZ_ERR_NOT_CONVERGED;
+    std::string message;
+    std::vector<SweepSlot> log;
+};
+
+// Scratch and table of one multi-field run; slot rows are sweep-major
+// (row k holds the slot of sweep k of every field).
+template <typename T>
+struct MultiRun {
+    explicit MultiRun(cudaStream_t st) : s(st), ws(st) {}
+    int setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweeps, int q, cudaStream_t s);
+    // One generation: the fused first pass of fields with `first` set, the
+    // detection of every other active field, then the edits of all active
+    // fields.  Clears `first` afterwards.
+    int generation();
+    // The remaining sweeps of all active fields in one cooperative launch.
+    int loop(int64_t *iters);
+    int read_row(int64_t k, std::vector<SweepSlot> &row);
+    int push_table();
+
+    cudaStream_t s;
+    Workspace ws;
+    int n = 0;
+    int64_t max_sweeps = 0;
+    int q = 5;
+    std::vector<Inst<T>> host;
+    std::vector<uint32_t> tpre, rpre;
+    uint32_t total_tiles = 0, total_rounds = 0;
+    Inst<T> *dinst = nullptr;
+    uint32_t *dtpre = nullptr, *drpre = nullptr;
+    long long *diters = nullptr;
+    SweepSlot *slots = nullptr;
+};
+
+// One generation over a device table of n fields (see MultiRun::generation),
+// and the gather of each field's current-sweep slot into out[0..n).
+template <typename T>
+int launch_generation(const Inst<T> *dinst, const uint32_t *dtpre, const uint32_t *drpre, int n,
+                      uint32_t total_tiles, uint32_t total_rounds, bool any_first, cudaStream_t s);
+template <typename T>
+int launch_gather(const Inst<T> *dinst, int n, SweepSlot *out, cudaStream_t s);
+
+// Scratch bytes of one field (codes, counters, proxies, three bitmaps) and
+// its sweep slots.
+inline size_t field_scratch_bytes(const Geom &g, int64_t max_sweeps) {
+    auto up = [](size_t b) { return (b + 255) & ~static_cast<size_t>(255); };
+    return up(g.n) * 2 + up(4 * g.n) + 3 * up(4 * g.nwords) + up(sizeof(SweepSlot) * static_cast<size_t>(max_sweeps));
+}
+
+template <typename T>
+int batch_impl(const std::vector<FieldSpec<T>> &specs, const pmsz_opts *opts, std::vector<BatchOutcome> &out,
+               cudaStream_t s);
+
+}  // namespace pmsz

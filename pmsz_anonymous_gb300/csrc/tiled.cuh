@@ -24,6 +24,8 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include "helpers.cuh"
+
 namespace cg = cooperative_groups;
 
 namespace pmsz {
@@ -101,16 +103,16 @@ __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; 
 //   kCodes : fa = a field; writes its code byte only (pmsz_codes_*).
 // ---------------------------------------------------------------------------
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
-                                                    uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
-                                                    uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
-                                                    SweepSlot *slot, Geom g) {
+__device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &sm, const T *__restrict__ fa,
+                                           const T *__restrict__ fb, uint8_t *__restrict__ codes,
+                                           uint32_t *__restrict__ hp, uint32_t *__restrict__ req,
+                                           uint32_t *__restrict__ act_next, SweepSlot *slot, const Geom &g, int bx,
+                                           int by, int bz) {
     constexpr int NF = MODE == kFirst ? 2 : 1;
     using K = typename KeyOf<T>::type;
-    __shared__ TileSmem<T, NF> sm;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
-    const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
-    const int zb = blockIdx.z * kZChunk, ze = min(g.nz, zb + kZChunk);
+    const int x0 = bx * kTX, y0 = by * kTY;
+    const int zb = bz * kZChunk, ze = min(g.nz, zb + kZChunk);
     const int x = x0 + tx, y = y0 + ty;
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
 
@@ -218,6 +220,15 @@ __global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa,
     if (MODE != kCodes) flush_counts(slot, cmax, cmin, cdir, active, bad);
 }
 
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
+                                                       uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
+                                                       uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                       SweepSlot *slot, Geom g) {
+    __shared__ TileSmem<T, MODE == kFirst ? 2 : 1> sm;
+    tiled_body<T, MODE>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // ---------------------------------------------------------------------------
 // Load policies.  Standalone sweep kernels read arrays that no thread of the
 // same launch writes through the read-only path (__ldg).  The persistent loop
@@ -283,14 +294,14 @@ __device__ __forceinline__ bool load_round(const uint32_t *__restrict__ bm, size
 // the bitmap); a true result sets the voxel's bit in a per-word result mask,
 // and flush(w, mask) is then called once per word with a non-zero mask, by the
 // thread that owns the word.  Every thread of the block must call this.
+// One round (2048 words from `base`) of for_each_set_bit.
 template <class L, class Work, class Flush>
-__device__ __forceinline__ void for_each_set_bit(ListSmem &sm, uint32_t *__restrict__ bm, const Geom &g, Work work,
-                                                 Flush flush) {
+__device__ __forceinline__ void process_round(ListSmem &sm, uint32_t *__restrict__ bm, const Geom &g, size_t base,
+                                              Work &work, Flush &flush) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    for (size_t base = static_cast<size_t>(blockIdx.x) * kRoundWords; base < g.nwords;
-         base += static_cast<size_t>(gridDim.x) * kRoundWords) {
+    {
         uint32_t w8[kWordsPerThread];
-        if (!load_round<L>(bm, base, g, w8)) continue;  // uniform
+        if (!load_round<L>(bm, base, g, w8)) return;  // uniform
         const size_t w0 = base + static_cast<size_t>(t) * kWordsPerThread;
         uint32_t c = 0;
 #pragma unroll
@@ -355,19 +366,30 @@ __device__ __forceinline__ void for_each_set_bit(ListSmem &sm, uint32_t *__restr
     }
 }
 
+template <class L, class Work, class Flush>
+__device__ __forceinline__ void for_each_set_bit(ListSmem &sm, uint32_t *__restrict__ bm, const Geom &g, Work &work,
+                                                 Flush &flush) {
+    for (size_t base = static_cast<size_t>(blockIdx.x) * kRoundWords; base < g.nwords;
+         base += static_cast<size_t>(gridDim.x) * kRoundWords)
+        process_round<L>(sm, bm, g, base, work, flush);
+}
+
 // ---------------------------------------------------------------------------
-// Sparse detection over the active bitmap, reading the proxy array of fhat.
-// Mismatching voxels are collected per word and written to act_next by the
-// word's owner thread (one writer per word).
+// Sparse detection of one voxel of the active set, reading the proxy array of
+// fhat (exact keys on a failed certificate), with the reference rules; the
+// word's mismatch bits go to act_next through DetectFlush (one writer per
+// word).  Counters accumulate in the functor.
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__device__ __forceinline__ void sparse_detect_body(ListSmem &sm, const T *__restrict__ fh, const uint32_t *__restrict__ hp,
-                                                   const uint8_t *__restrict__ codes, uint32_t *__restrict__ act_cur,
-                                                   uint32_t *__restrict__ act_next, uint32_t *__restrict__ req,
-                                                   SweepSlot *slot, const Geom &g) {
-    const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
+struct DetectWork {
+    const T *fh;
+    const uint32_t *hp;
+    const uint8_t *codes;
+    uint32_t *req;
+    Geom g;
     uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
-    auto work = [&](int x, int y, int z, uint32_t) -> bool {
+    __device__ __forceinline__ bool operator()(int x, int y, int z, uint32_t) {
+        const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
         const size_t i = flat(g, x, y, z);
         const bool interior = x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
         const uint32_t valid = interior ? kAllValid : valid_mask(x, y, z, g.nx, g.ny, g.nz);
@@ -394,10 +416,27 @@ __device__ __forceinline__ void sparse_detect_body(ListSmem &sm, const T *__rest
         ++active;
         if (tm) request_targets(req, g, x, y, z, tm);
         return tm != 0;
-    };
-    auto flush = [&](size_t w, uint32_t m) { act_next[w] = m; };
+    }
+    __device__ __forceinline__ void flush_to(SweepSlot *slot) {
+        flush_counts(slot, cmax, cmin, cdir, active, 0);
+        cmax = cmin = cdir = active = 0;
+    }
+};
+
+struct DetectFlush {
+    uint32_t *act_next;
+    __device__ __forceinline__ void operator()(size_t w, uint32_t m) { act_next[w] = m; }
+};
+
+template <class L, typename T>
+__device__ __forceinline__ void sparse_detect_body(ListSmem &sm, const T *__restrict__ fh, const uint32_t *__restrict__ hp,
+                                                   const uint8_t *__restrict__ codes, uint32_t *__restrict__ act_cur,
+                                                   uint32_t *__restrict__ act_next, uint32_t *__restrict__ req,
+                                                   SweepSlot *slot, const Geom &g) {
+    DetectWork<L, T> work{fh, hp, codes, req, g};
+    DetectFlush flush{act_next};
     for_each_set_bit<L>(sm, act_cur, g, work, flush);
-    flush_counts(slot, cmax, cmin, cdir, active, 0);
+    work.flush_to(slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -405,17 +444,20 @@ __device__ __forceinline__ void sparse_detect_body(ListSmem &sm, const T *__rest
 // every requested vertex, in T:
 //   if |f - (fhat - delta)| <= eps && cnt < q-1 { fhat -= delta; cnt++ }
 //   else { cnt = q; fhat = f - eps }
-// the proxy of every changed value refreshed, and the closed stencil of the
-// changed vertices (collected per word) marked in act_next by the word's
-// owner thread.
+// the proxy of every changed value refreshed; ApplyFlush marks the closed
+// stencil of the changed vertices of a word in act_next (owner thread).
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f, T *__restrict__ fh,
-                                           uint8_t *__restrict__ cnt, uint32_t *__restrict__ hp,
-                                           uint32_t *__restrict__ req, uint32_t *__restrict__ act_next, SweepSlot *slot,
-                                           const Geom &g, T eps, T delta, int q) {
-    uint32_t nreq = 0, nchg = 0, nprog = 0;
-    auto work = [&](int x, int y, int z, uint32_t) -> bool {
+struct ApplyWork {
+    const T *f;
+    T *fh;
+    uint8_t *cnt;
+    uint32_t *hp;
+    Geom g;
+    T eps, delta;
+    int q;
+    uint32_t nreq = 0, nprog = 0;
+    __device__ __forceinline__ bool operator()(int x, int y, int z, uint32_t) {
         const size_t v = flat(g, x, y, z);
         const T old = L::ld(fh + v);
         const uint8_t oc = L::ld(cnt + v);
@@ -437,14 +479,22 @@ __device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f
         ++nreq;
         nprog += (chg || nc != oc) ? 1u : 0u;
         return chg;
-    };
-    auto flush = [&](size_t w, uint32_t m) {
+    }
+};
+
+struct ApplyFlush {
+    uint32_t *act_next;
+    Geom g;
+    uint32_t nchg = 0;
+    __device__ __forceinline__ void operator()(size_t w, uint32_t m) {
         nchg += __popc(m);
         int wx, y, z;
         word_coords(g, w, wx, y, z);
         mark_stencil(act_next, g, wx, y, z, m);
-    };
-    for_each_set_bit<L>(sm, req, g, work, flush);
+    }
+};
+
+__device__ __forceinline__ void flush_apply_counts(SweepSlot *slot, uint32_t nreq, uint32_t nchg, uint32_t nprog) {
     nreq = warp_sum_u32(nreq);
     nchg = warp_sum_u32(nchg);
     nprog = warp_sum_u32(nprog);
@@ -453,6 +503,17 @@ __device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f
         if (nchg) atomicAdd(&slot->changed, (unsigned long long)nchg);
         if (nprog) atomicAdd(&slot->progressed, (unsigned long long)nprog);
     }
+}
+
+template <class L, typename T>
+__device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f, T *__restrict__ fh,
+                                           uint8_t *__restrict__ cnt, uint32_t *__restrict__ hp,
+                                           uint32_t *__restrict__ req, uint32_t *__restrict__ act_next, SweepSlot *slot,
+                                           const Geom &g, T eps, T delta, int q) {
+    ApplyWork<L, T> work{f, fh, cnt, hp, g, eps, delta, q};
+    ApplyFlush flush{act_next, g};
+    for_each_set_bit<L>(sm, req, g, work, flush);
+    flush_apply_counts(slot, work.nreq, flush.nchg, work.nprog);
 }
 
 template <typename T>
