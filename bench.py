@@ -9,11 +9,16 @@ normalised to [0,1]) decompressed through the ZFP-like stand-in at eps = 1e-4
 value   device-resident throughput, Gvox/s = N / (device time of one
         pmsz_correct call), CUDA events on the launching stream, fhat refreshed
         from a pristine device copy before each step (untimed).
-e2e     the same through the C ABI with host buffers: pinned host f and fhat
-        copied in, pmsz_correct, the corrected field copied back, all timed.
-roofline  the fused labelling + first detection pass (the dominant kernel):
-        algorithmic bytes N*(2*sizeof(T)+1) / its event-timed duration,
-        against the measured HBM copy bandwidth.
+e2e     the same through the host-buffer C ABI (pmsz_correct_host_*): pinned
+        host f and fhat copied in, the correction, the edit extraction and the
+        copy back of what the reference's main hands to its host encoder --
+        the delta symbols (1 B/voxel) and the clamp list -- all timed.
+roofline  the fused labelling + first detection pass k_tiled<T,kFirst> (the
+        largest kernel, about 40 % of a call): algorithmic bytes
+        2*N*(sizeof(T)+1) -- the one-time original labelling (read f, write
+        the code byte) plus one detection sweep (read fhat and the code byte)
+        -- over its event-timed duration, against the measured HBM copy
+        bandwidth; traffic = ncu dram bytes per launch of the same kernel.
 cpu_baseline  the CPU oracle (a restatement of the reference loop, OpenMP on
         all host cores) on a z-slab sample of the same field.
 
@@ -257,21 +262,21 @@ def run_ours(args):
         ms = float(t.item())
     value = world * n / (ms * 1e-3) / 1e9
 
-    # e2e through the C ABI from pinned host buffers
+    # e2e through the host-buffer C ABI (pmsz_correct_host_*): pinned host f and
+    # fhat copied in, correction, edit extraction, and the reference main's
+    # host output -- the delta symbols and the clamp list -- copied back.
     f_h = f.cpu().pin_memory()
     fh_h = fh0.cpu().pin_memory()
-    out_h = torch.empty_like(fh_h).pin_memory()
-    fd, fhd = torch.empty_like(f), torch.empty_like(fh0)
-    e2e_times = []
+    deltas_h = torch.empty(n, dtype=torch.uint8).pin_memory()
+    clamp_h = torch.empty(n, dtype=f.dtype).pin_memory()
+    e2e_times, n_clamp, e2e_res = [], 0, None
     for i in range(1 + args.e2e_steps if args.e2e_steps > 0 else 0):
         barrier()
         start.record()
-        fd.copy_(f_h, non_blocking=True)
-        fhd.copy_(fh_h, non_blocking=True)
-        api.correct(fd, fhd, args.eb)
-        out_h.copy_(fhd, non_blocking=True)
+        e2e_res, extra = api.correct_host(f_h, fh_h, args.eb, deltas=deltas_h, clamp=clamp_h, edits_only=True)
         stop.record()
         stop.synchronize()
+        n_clamp = extra["n_clamp"]
         if i:
             e2e_times.append(start.elapsed_time(stop))
     e2e_ms = statistics.mean(e2e_times) if e2e_times else float("nan")
@@ -279,10 +284,12 @@ def run_ours(args):
         t = torch.tensor([e2e_ms], device=device, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    ok = api.verify(f, fhd if e2e_times else fh, args.eb)
+    if e2e_res is not None and (e2e_res.sweeps != last.sweeps or e2e_res.edits != last.edits):
+        raise RuntimeError("host-buffer call disagrees with the device-buffer call")
+    ok = api.verify(f, fh, args.eb)
 
     peak, peak_kind = measured_peaks()
-    bytes_first = n * (2 * itemsize + 1)
+    bytes_first = 2 * n * (itemsize + 1)
     achieved = bytes_first / (statistics.mean(first_ms) * 1e-3) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": "Gvox/s", "n_gpus": world, "steps": args.steps,
@@ -297,12 +304,14 @@ def run_ours(args):
                                          "active_per_sweep": [int(v) for v in last.log[:, 6]],
                                          "requested_per_sweep": [int(v) for v in last.log[:, 3]]}),
         "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n * itemsize},
-        "roofline": {"bound": "hbm", "kernel": "k_detect_full<T,true> (labelling + first detection)",
+                "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n + n_clamp * itemsize,
+                "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY: H2D f and fhat, correction, "
+                        "edit extraction, D2H delta symbols (1 B/voxel) and clamp list"},
+        "roofline": {"bound": "hbm", "kernel": "k_tiled<T,kFirst> (labelling + first detection)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": bytes_first,
                      "ms_per_launch": statistics.mean(first_ms),
-                     "traffic": profiled_traffic(f"first_pass_{args.dtype}")},
+                     "traffic": profiled_traffic(f"first_pass_{args.shape.replace(',', 'x')}_{args.dtype}")},
         "gpu_launches": launches,
         "verify": ok,
     }

@@ -37,6 +37,14 @@ extern "C" {
 #define PMSZ_FLAG_TIMING 2u       /* record CUDA events around every kernel on
                                      `stream` and report per-kernel device time
                                      in pmsz_result */
+#define PMSZ_FLAG_EDITS_ONLY 4u   /* pmsz_correct_host_*: hand back only the
+                                     edit output (deltas, clamp list) the
+                                     reference's main copies to the host
+                                     (pMSz.cu:2429-2543) and leave the host
+                                     fhat unchanged */
+#define PMSZ_FLAG_NAIVE 8u        /* pmsz_correct_host_*: run the naive-MSz
+                                     strategy (pmsz_correct_naive_*) instead of
+                                     the pMSz loop */
 
 typedef struct pmsz_opts {
     int32_t q;           /* edit levels; the reference hard-codes q = 5 (pMSz.cu:2630) */
@@ -109,6 +117,32 @@ int pmsz_correct_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t n
                      double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
 int pmsz_correct_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz,
                      double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
+
+/*
+ * pmsz_correct_naive_{f32,f64}: the naive-MSz strategy, replacing c_loops of
+ * naive_MSz.cu (naive_MSz.cu:1887-2220), the reference's second program.  One
+ * outer iteration runs extrema-only sweeps (false / missing maxima and minima,
+ * no direction rule; naive_MSz.cu:776-826) until one finds none, then one
+ * integral-path repair -- AS / DS labels of the current field by pointer
+ * jumping, and for every voxel whose label differs from the original's a walk
+ * along the agreeing directions to the first divergence, where one vertex is
+ * lowered (extract_false_path, naive_MSz.cu:1767-1864) -- then a check that
+ * counts false extrema and label mismatches; the loop ends when the check
+ * finds none.  The result preserves the extrema and both segmentations (not
+ * every steepest direction, which pmsz_correct_* also preserves).  Same
+ * arguments, scratch rules and edit arithmetic as pmsz_correct_*.  Records in
+ * res->sweep_log: one per extrema sweep {fmax, fmin, 0, requested, changed},
+ * one per path repair {0, 0, label mismatches, requested, changed}, one per
+ * check {fmax, fmin, voxels with a DS (else AS) label mismatch, 0, 0};
+ * res->iteration is the reference's `ite` (2 per outer iteration plus 1 per
+ * extrema sweep).  Needs nx*ny*nz < 2^32.  Returns PMSZ_ERR_NOT_CONVERGED at
+ * max_sweeps records, when an extrema sweep changes nothing, or when a whole
+ * outer iteration changes nothing (the reference would loop forever).
+ */
+int pmsz_correct_naive_f32(const float *f, float *fhat, size_t nx, size_t ny, size_t nz,
+                           double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
+int pmsz_correct_naive_f64(const double *f, double *fhat, size_t nx, size_t ny, size_t nz,
+                           double eb, const pmsz_opts *opts, pmsz_result *res, void *stream);
 
 /*
  * pmsz_correct_noalloc: the same correction as pmsz_correct_{f32,f64}, but

@@ -6,6 +6,8 @@
   SZ3, ZFP and zstd (the cubin keeps only the kernels; nothing of those
   libraries is called).  Built only where the reference sources exist; the
   cubin then travels with the repository copy.
+* ``oracle/_ref/naive_ref.cubin`` -- the unmodified ``naive_MSz.cu``, the
+  same way.
 * ``oracle/_ref/ref_harness`` -- ``oracle/ref_harness.cpp`` (driver API),
   compiled on the machine that runs it.
 
@@ -22,6 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF_SRC = "/root/reference/pMSz.cu"
 CUBIN = os.path.join(OUT, "pmsz_ref.cubin")
+NAIVE_SRC = "/root/reference/naive_MSz.cu"
+NAIVE_CUBIN = os.path.join(OUT, "naive_ref.cubin")
 HARNESS = os.path.join(OUT, "ref_harness")
 
 
@@ -30,15 +34,21 @@ def _cuda_home() -> str:
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
 
 
-def build_cubin() -> str | None:
-    if not os.path.exists(REF_SRC):
-        return CUBIN if os.path.exists(CUBIN) else None
+def _cubin(src: str, out: str) -> str | None:
+    if not os.path.exists(src):
+        return out if os.path.exists(out) else None
     os.makedirs(OUT, exist_ok=True)
-    if not os.path.exists(CUBIN) or os.path.getmtime(CUBIN) < os.path.getmtime(REF_SRC):
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
         cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
-               "-std=c++17", "-I" + os.path.join(HERE, "ref_shim"), REF_SRC, "-o", CUBIN]
+               "-std=c++17", "-I" + os.path.join(HERE, "ref_shim"), src, "-o", out]
         subprocess.run(cmd, check=True, capture_output=True, text=True)
-    return CUBIN
+    return out
+
+
+def build_cubin() -> str | None:
+    """pMSz.cu -> pmsz_ref.cubin, and naive_MSz.cu -> naive_ref.cubin."""
+    _cubin(NAIVE_SRC, NAIVE_CUBIN)
+    return _cubin(REF_SRC, CUBIN)
 
 
 def build_harness() -> str:

@@ -62,6 +62,8 @@ def lib():
                 getattr(L, f"pmszo_extract_edits_{suf}").argtypes = [
                     _P, _P, _P, _I64, ctypes.c_double, ctypes.c_int, _P, _P,
                     _P, _P]
+                getattr(L, f"pmszo_correct_naive_{suf}").argtypes = [
+                    _P, _P, _I64, _I64, _I64, ctypes.c_double, ctypes.c_int, _I64, _P, _P, _P]
                 getattr(L, f"pmszo_reconstruct_{suf}").argtypes = [
                     _P, _P, _P, _I64, _I64, ctypes.c_double, ctypes.c_int, _P]
             L.pmszo_path_compress.argtypes = [_P, _P, _I64]
@@ -135,6 +137,26 @@ def correct(f: np.ndarray, fhat: np.ndarray, eb: float, q: int = 5,
     n = int(res.sweeps)
     recs = np.array([[log[i].fmax, log[i].fmin, log[i].fdir, log[i].requested,
                       log[i].changed] for i in range(n)], dtype=np.uint64).reshape(n, 5)
+    return out, cnt.reshape(f.shape), int(res.status), n, recs
+
+
+def correct_naive(f: np.ndarray, fhat: np.ndarray, eb: float, q: int = 5, max_sweeps: int = 100000):
+    """naive-MSz loop (naive_MSz.cu:1887-2220), snapshot semantics; same
+    return convention as correct()."""
+    f = np.ascontiguousarray(f)
+    out = np.array(fhat, dtype=f.dtype, copy=True, order="C")
+    nx, ny, nz = _dims(f)
+    cnt = np.zeros(f.size, np.uint8)
+    log = (SweepRecord * int(max_sweeps))()
+    res = Result()
+    rc = getattr(lib(), f"pmszo_correct_naive_{_suf(f)}")(
+        _ptr(f), _ptr(out), nx, ny, nz, float(eb), int(q), int(max_sweeps), _ptr(cnt),
+        ctypes.cast(log, _P), ctypes.byref(res))
+    if rc not in (OK, ERR_NOT_CONVERGED):
+        raise ValueError(f"correct_naive failed: {rc}")
+    n = int(res.sweeps)
+    recs = np.array([[log[i].fmax, log[i].fmin, log[i].fdir, log[i].requested, log[i].changed]
+                     for i in range(n)], dtype=np.uint64).reshape(n, 5)
     return out, cnt.reshape(f.shape), int(res.status), n, recs
 
 

@@ -504,3 +504,165 @@ int pmszo_unpack_nbits(const uint8_t *packed, int64_t packed_bytes, int64_t n,
     }
     return PMSZO_OK;
 }
+
+/* ---------------------------------------------------------------------- */
+/* naive-MSz correction: naive_MSz.cu c_loops (1887-2220) with its         */
+/* extrema-only iscriticle (645-850) and extract_false_path (1767-1864),   */
+/* under snapshot semantics.  One outer iteration:                          */
+/*   - extrema sweeps (rules R1/R2 only) while the last count of false or  */
+/*     missing extrema is non-zero (initially: at least one sweep);         */
+/*   - a path sweep: labels of the current field by path compression; for */
+/*     every voxel whose DS (AS) label differs from the original's, walk   */
+/*     the steps on which the original and current directions agree to the */
+/*     first divergence and lower the original descent neighbour there     */
+/*     (resp. the current ascent neighbour); fdir counts each mismatch;    */
+/*   - a check: extremum counts and, per voxel, one count if its DS label   */
+/*     differs, else one if its AS label differs (fix=1 mode).              */
+/* The loop ends when the check is all zero.  Records: extrema sweep        */
+/* {fmax,fmin,0,req,chg}, path sweep {0,0,fdir,req,chg}, check              */
+/* {fmax,fmin,fdir,0,0}.  Walks follow or_types literally, including its    */
+/* encoding of maxima (slot 1 = descent) and minima (slot 0 = -2); a walk   */
+/* that would target the -2 marker (the reference would index edits[-2])   */
+/* edits nothing.  Walks are bounded by n steps; an outer iteration that   */
+/* changes nothing ends the loop with PMSZO_ERR_NOT_CONVERGED.              */
+/* ---------------------------------------------------------------------- */
+static inline int64_t pmszo_or0(const int64_t *oasc, const int64_t *odesc, int64_t c) {
+    if (oasc[c] == c) return -1;          /* original maximum */
+    if (odesc[c] == c) return -2;         /* original minimum */
+    return odesc[c];
+}
+static inline int64_t pmszo_or1(const int64_t *oasc, const int64_t *odesc, int64_t c) {
+    return oasc[c] == c ? odesc[c] : oasc[c];
+}
+
+/* DS walk from i; returns the vertex to lower or -1. */
+static int64_t pmszo_walk_ds(const int64_t *oasc, const int64_t *odesc, const int64_t *cdesc, int64_t i, int64_t n) {
+    int64_t cur = i;
+    for (int64_t steps = 0;; ++steps) {
+        const int64_t s0 = pmszo_or0(oasc, odesc, cur);
+        if (s0 != cdesc[cur]) break;
+        if (cdesc[cur] == cur && s0 == cur) return -1;
+        if (s0 == cur) break;
+        cur = s0;
+        if (steps > n) return -1;
+    }
+    const int64_t fls = cdesc[cur];
+    const int64_t tru = oasc[cur] == cur ? odesc[cur] : pmszo_or0(oasc, odesc, cur);
+    return (tru >= 0 && fls != tru) ? tru : -1;
+}
+
+/* AS walk from i; returns the vertex to lower or -1. */
+static int64_t pmszo_walk_as(const int64_t *oasc, const int64_t *odesc, const int64_t *casc, int64_t i, int64_t n) {
+    int64_t cur = i;
+    for (int64_t steps = 0;; ++steps) {
+        const int64_t s1 = pmszo_or1(oasc, odesc, cur);
+        if (s1 != casc[cur]) break;
+        if (casc[cur] == cur && s1 == cur) return -1;
+        if (s1 == cur) break;
+        cur = s1;
+        if (steps > n) return -1;
+    }
+    const int64_t fls = casc[cur], tru = pmszo_or1(oasc, odesc, cur);
+    return fls != tru ? fls : -1;
+}
+
+#define PMSZO_DEFINE_NAIVE(T, SUF)                                                                   \
+    int pmszo_correct_naive_##SUF(const T *f, T *fh, int64_t nx, int64_t ny, int64_t nz, double eb,  \
+                                  int q, int64_t max_sweeps, uint8_t *cnt_out, pmszo_sweep_t *log,   \
+                                  pmszo_result_t *res) {                                             \
+        if (nx <= 0 || ny <= 0 || nz <= 0 || !(eb > 0) || q < 1 || q > 255 || max_sweeps < 1)        \
+            return PMSZO_ERR_ARG;                                                                    \
+        const int64_t n = nx * ny * nz;                                                              \
+        const T eps = (T)eb, delta = (T)(eb / (double)q);                                            \
+        int64_t *oa = malloc((size_t)n * 8), *od = malloc((size_t)n * 8), *ca = malloc((size_t)n * 8); \
+        int64_t *cd = malloc((size_t)n * 8), *as0 = malloc((size_t)n * 8), *ds0 = malloc((size_t)n * 8); \
+        int64_t *as1 = malloc((size_t)n * 8), *ds1 = malloc((size_t)n * 8);                          \
+        uint8_t *req = calloc((size_t)n, 1), *cnt = cnt_out ? cnt_out : malloc((size_t)n);           \
+        int status = PMSZO_ERR_OOM;                                                                  \
+        int64_t nrec = 0, edits = 0;                                                                 \
+        if (!oa || !od || !ca || !cd || !as0 || !ds0 || !as1 || !ds1 || !req || !cnt) goto done;     \
+        memset(cnt, 0, (size_t)n);                                                                   \
+        pmszo_label_##SUF(f, nx, ny, nz, oa, od);                                                    \
+        pmszo_path_compress(oa, as0, n);                                                             \
+        pmszo_path_compress(od, ds0, n);                                                             \
+        status = PMSZO_ERR_NOT_CONVERGED;                                                            \
+        uint64_t hmax = 1, hmin = 1;                                                                 \
+        for (;;) {                                                                                   \
+            uint64_t progressed_outer = 0;                                                           \
+            while (hmax || hmin) { /* extrema sweeps */                                             \
+                if (nrec >= max_sweeps) goto done;                                                   \
+                pmszo_label_##SUF(fh, nx, ny, nz, ca, cd);                                           \
+                uint64_t cmax = 0, cmin = 0;                                                         \
+                for (int64_t i = 0; i < n; ++i) {                                                    \
+                    const int is_max = ca[i] == i, is_min = cd[i] == i;                              \
+                    const int omax = oa[i] == i, omin = !omax && od[i] == i;                         \
+                    if (is_max != omax) { ++cmax; req[omax ? ca[i] : i] = 1; }                       \
+                    if (is_min != omin) { ++cmin; req[omin ? i : od[i]] = 1; }                       \
+                }                                                                                    \
+                uint64_t rq = 0, ch = 0, pr = 0;                                                     \
+                for (int64_t v = 0; v < n; ++v) {                                                    \
+                    if (!req[v]) continue;                                                           \
+                    req[v] = 0; ++rq; int vc = 0;                                                    \
+                    pr += (uint64_t)pmszo_apply_##SUF(f, fh, cnt, v, eps, delta, q, &vc);            \
+                    ch += (uint64_t)vc;                                                              \
+                }                                                                                    \
+                if (log) { pmszo_sweep_t r = {cmax, cmin, 0, rq, ch}; log[nrec] = r; }               \
+                ++nrec; edits += (int64_t)rq; progressed_outer += pr;                                \
+                hmax = cmax; hmin = cmin;                                                            \
+                if ((cmax || cmin) && pr == 0) goto done; /* stuck */                                \
+            }                                                                                        \
+            /* path sweep */                                                                         \
+            if (nrec >= max_sweeps) goto done;                                                       \
+            pmszo_label_##SUF(fh, nx, ny, nz, ca, cd);                                               \
+            pmszo_path_compress(ca, as1, n);                                                         \
+            pmszo_path_compress(cd, ds1, n);                                                         \
+            uint64_t fdir = 0;                                                                       \
+            for (int64_t i = 0; i < n; ++i) {                                                        \
+                if (ds0[i] != ds1[i]) {                                                              \
+                    ++fdir;                                                                          \
+                    const int64_t t = pmszo_walk_ds(oa, od, cd, i, n);                               \
+                    if (t >= 0) req[t] = 1;                                                          \
+                }                                                                                    \
+                if (as0[i] != as1[i]) {                                                              \
+                    ++fdir;                                                                          \
+                    const int64_t t = pmszo_walk_as(oa, od, ca, i, n);                               \
+                    if (t >= 0) req[t] = 1;                                                          \
+                }                                                                                    \
+            }                                                                                        \
+            uint64_t rq = 0, ch = 0, pr = 0;                                                         \
+            for (int64_t v = 0; v < n; ++v) {                                                        \
+                if (!req[v]) continue;                                                               \
+                req[v] = 0; ++rq; int vc = 0;                                                        \
+                pr += (uint64_t)pmszo_apply_##SUF(f, fh, cnt, v, eps, delta, q, &vc);                \
+                ch += (uint64_t)vc;                                                                  \
+            }                                                                                        \
+            if (log) { pmszo_sweep_t r = {0, 0, fdir, rq, ch}; log[nrec] = r; }                      \
+            ++nrec; edits += (int64_t)rq; progressed_outer += pr;                                    \
+            /* check */                                                                              \
+            if (nrec >= max_sweeps) goto done;                                                       \
+            pmszo_label_##SUF(fh, nx, ny, nz, ca, cd);                                               \
+            pmszo_path_compress(ca, as1, n);                                                         \
+            pmszo_path_compress(cd, ds1, n);                                                         \
+            uint64_t cmax = 0, cmin = 0, cdir = 0;                                                   \
+            for (int64_t i = 0; i < n; ++i) {                                                        \
+                const int is_max = ca[i] == i, is_min = cd[i] == i;                                  \
+                const int omax = oa[i] == i, omin = !omax && od[i] == i;                             \
+                cmax += is_max != omax;                                                              \
+                cmin += is_min != omin;                                                              \
+                cdir += (ds0[i] != ds1[i]) || (as0[i] != as1[i]);                                    \
+            }                                                                                        \
+            if (log) { pmszo_sweep_t r = {cmax, cmin, cdir, 0, 0}; log[nrec] = r; }                  \
+            ++nrec;                                                                                  \
+            if (!cmax && !cmin && !cdir) { status = PMSZO_OK; goto done; }                           \
+            if (!progressed_outer) goto done; /* nothing can change any more */                     \
+            hmax = cmax; hmin = cmin;                                                                \
+        }                                                                                            \
+    done:                                                                                            \
+        if (res) { res->sweeps = nrec; res->edits_applied = edits; res->status = status; }           \
+        free(oa); free(od); free(ca); free(cd); free(as0); free(ds0); free(as1); free(ds1); free(req); \
+        if (!cnt_out) free(cnt);                                                                     \
+        return status;                                                                               \
+    }
+
+PMSZO_DEFINE_NAIVE(float, f32)
+PMSZO_DEFINE_NAIVE(double, f64)

@@ -14,6 +14,12 @@
 //   ref_harness <cubin> detect  <nx> <ny> <nz> <eb> <f.bin> <fh.bin> <out>
 //   ref_harness <cubin> correct <nx> <ny> <nz> <eb> <f.bin> <fh.bin> <out>
 //   ref_harness <cubin> extract <nx> <ny> <nz> <eb> <f.bin> <prev.bin> <out> <cur.bin>
+//   ref_harness <naive cubin> naive <nx> <ny> <nz> <eb> <f.bin> <fh.bin> <out>
+//
+// The naive mode loads oracle/_ref/naive_ref.cubin (the unmodified
+// naive_MSz.cu, compiled the same way) and restates the host sequence of its
+// c_loops (naive_MSz.cu:1887-2220) around its iscriticle<double>,
+// PathCompression, extract_false_path<double>, init_counter and init_edits.
 //
 // Outputs (raw little-endian, padded unless noted): <out>_ortypes.bin (int32,
 // 2 per voxel), <out>_dir_as.bin / _dir_ds.bin (int32), <out>_counts.bin
@@ -34,6 +40,10 @@ const char *kIscriticle = "_Z10iscriticleIdEvPiS0_S0_S0_PmPT_S3_S0_PhmmmmS0_mmmm
 const char *kInitCounter = "_Z12init_countermPh";
 const char *kInitEdits = "_Z10init_editsmPi";
 const char *kExtract = "_Z20extract_edits_kernelIdEvPKT_S2_S2_PKhPmPhPS0_mmmmmiS0_mPjS0_i";
+// naive_MSz.cu's kernels (its iscriticle has no max-only flag: 30 parameters)
+const char *kNaiveIscriticle = "_Z10iscriticleIdEvPiS0_S0_S0_PmPT_S3_S0_PhmmmmS0_mmmmmiS0_iS2_S2_iS2_S2_iii";
+const char *kPathCompression = "_Z15PathCompressionPimmmmi";
+const char *kFalsePath = "_Z18extract_false_pathIdEvPT_S1_PiS2_S2_S2_mmmmS2_S2_S2_S2_PhiS0_S0_iiS2_i";
 const double kInvalid = 1e30;
 
 #define CK(x)                                                                      \
@@ -70,7 +80,7 @@ void write(const std::string &path, const T *p, size_t n) {
 
 struct Ref {
     CUmodule mod;
-    CUfunction isc, initc, inite, extract;
+    CUfunction isc, initc, inite, extract, pathc, falsep;
     CUdeviceptr g_max, g_min, g_dir;
     size_t W, H, D, N;  // padded sizes
     unsigned grid;
@@ -105,11 +115,54 @@ void iscriticle(Ref &r, CUdeviceptr dir_as, CUdeviceptr dir_ds, CUdeviceptr inpu
     CK(cuCtxSynchronize());
 }
 
+// naive_MSz.cu's iscriticle (naive_MSz.cu:645-651): DS_M / AS_M first, and
+// data_type, preserveMSS, checkFinal last.
+void naive_iscriticle(Ref &r, CUdeviceptr dsm, CUdeviceptr asm_, CUdeviceptr dir_as, CUdeviceptr dir_ds,
+                      CUdeviceptr input, CUdeviceptr decp, CUdeviceptr edits, CUdeviceptr cnt, CUdeviceptr or_types,
+                      CUdeviceptr send_flag, int q, double bound, double delta, int ite, int data_type,
+                      int check_final, size_t nx, size_t ny) {
+    CUdeviceptr nullp = 0;
+    size_t W = r.W, H = r.H, D = r.D, N = r.N, zero = 0, wt = nx, ht = ny;
+    int rank = 0, preserve = 0;
+    double uth = 0.0, lth = 0.0;
+    void *args[] = {&dsm, &asm_, &dir_as, &dir_ds, &nullp, &input, &decp, &edits, &cnt, &W, &H, &D, &N,
+                    &or_types, &zero, &zero, &zero, &wt, &ht, &rank, &send_flag, &q, &bound, &delta, &ite, &uth,
+                    &lth, &data_type, &preserve, &check_final};
+    CK(cuLaunchKernel(r.isc, r.grid, 1, 1, 256, 1, 1, 0, 0, args, nullptr));
+    CK(cuCtxSynchronize());
+}
+
+void path_compression(Ref &r, CUdeviceptr label) {
+    size_t N = r.N, W = r.W, H = r.H, D = r.D;
+    int preserve = 0;  // c_loops passes 0 (naive_MSz.cu:1914-1917, 2045-2047)
+    void *args[] = {&label, &N, &W, &H, &D, &preserve};
+    CK(cuLaunchKernel(r.pathc, r.grid, 1, 1, 256, 1, 1, 0, 0, args, nullptr));
+    CK(cuCtxSynchronize());
+}
+
+void false_path(Ref &r, CUdeviceptr decp, CUdeviceptr input, CUdeviceptr dsm0, CUdeviceptr dsm1, CUdeviceptr asm0,
+                CUdeviceptr asm1, CUdeviceptr or_types, CUdeviceptr dir_ds, CUdeviceptr dir_as, CUdeviceptr edits,
+                CUdeviceptr cnt, int q, double bound, double delta, int ite, CUdeviceptr send_flag, int fix) {
+    size_t N = r.N, W = r.W, H = r.H, D = r.D;
+    int rank = 0;
+    void *args[] = {&decp, &input, &dsm0, &dsm1, &asm0, &asm1, &N, &W, &H, &D, &or_types, &dir_ds, &dir_as,
+                    &edits, &cnt, &q, &bound, &delta, &rank, &ite, &send_flag, &fix};
+    CK(cuLaunchKernel(r.falsep, r.grid, 1, 1, 256, 1, 1, 0, 0, args, nullptr));
+    CK(cuCtxSynchronize());
+}
+
+void init_edits(Ref &r, CUdeviceptr edits) {
+    size_t ds = r.N;
+    void *a[] = {&ds, &edits};
+    CK(cuLaunchKernel(r.inite, r.grid, 1, 1, 256, 1, 1, 0, 0, a, nullptr));
+    CK(cuCtxSynchronize());
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
     if (argc < 10) {
-        std::fprintf(stderr, "usage: ref_harness <cubin> <label|detect|correct|extract> nx ny nz eb f.bin fh.bin out [cur.bin]\n");
+        std::fprintf(stderr, "usage: ref_harness <cubin> <label|detect|correct|extract|naive> nx ny nz eb f.bin fh.bin out [cur.bin]\n");
         return 2;
     }
     const std::string mode = argv[2];
@@ -128,11 +181,16 @@ int main(int argc, char **argv) {
     CK(cuDevicePrimaryCtxRetain(&ctx, dev));
     CK(cuCtxSetCurrent(ctx));
     Ref r;
+    const bool naive = mode == "naive";
     CK(cuModuleLoad(&r.mod, argv[1]));
-    CK(cuModuleGetFunction(&r.isc, r.mod, kIscriticle));
+    CK(cuModuleGetFunction(&r.isc, r.mod, naive ? kNaiveIscriticle : kIscriticle));
     CK(cuModuleGetFunction(&r.initc, r.mod, kInitCounter));
     CK(cuModuleGetFunction(&r.inite, r.mod, kInitEdits));
     CK(cuModuleGetFunction(&r.extract, r.mod, kExtract));
+    if (naive) {
+        CK(cuModuleGetFunction(&r.pathc, r.mod, kPathCompression));
+        CK(cuModuleGetFunction(&r.falsep, r.mod, kFalsePath));
+    }
     size_t gsz;
     CK(cuModuleGetGlobal(&r.g_max, &gsz, r.mod, "count_f_max"));
     CK(cuModuleGetGlobal(&r.g_min, &gsz, r.mod, "count_f_min"));
@@ -200,6 +258,83 @@ int main(int argc, char **argv) {
         write(out + "_deltas.bin", deltas.data(), n);
         write(out + "_editsout.bin", eo.data(), n);
         write(out + "_hcount.bin", &hc, 1);
+        return 0;
+    }
+
+    if (naive) {
+        // c_loops of naive_MSz.cu at one rank (naive_MSz.cu:1887-2220); the halo
+        // exchange has no neighbour to talk to.  d_as / d_ds hold the current
+        // directions, DS_M / AS_M the original labels, dec_* the current ones.
+        CUdeviceptr dsm, asm0, dsm1, asm1;
+        CK(cuMemAlloc(&dsm, r.N * 4));
+        CK(cuMemAlloc(&asm0, r.N * 4));
+        CK(cuMemAlloc(&dsm1, r.N * 4));
+        CK(cuMemAlloc(&asm1, r.N * 4));
+        CK(cuMemsetD32(dsm, 0, r.N));
+        CK(cuMemsetD32(asm0, 0, r.N));
+        CK(cuMemsetD32(dsm1, 0, r.N));
+        CK(cuMemsetD32(asm1, 0, r.N));
+        {
+            size_t ds = r.N;
+            void *args[] = {&ds, &d_cnt};
+            CK(cuLaunchKernel(r.initc, r.grid, 1, 1, 256, 1, 1, 0, 0, args, nullptr));
+            CK(cuCtxSynchronize());
+        }
+        int ite = 0;
+        naive_iscriticle(r, dsm, asm0, d_as, d_ds, d_in, d_in, d_edits, d_cnt, d_or, d_flag, q, bound, delta, ite, 1, 0,
+                         nx, ny);
+        path_compression(r, dsm);
+        path_compression(r, asm0);
+        unsigned c[3] = {0, 0, 0};
+        unsigned gmax = 1, gmin = 1, gdir = 0, hmax = 1, hmin = 1;
+        int inner = 0, outer = 0;
+        std::vector<unsigned> recs;  // per pass: kind, fmax, fmin, fdir (kind 0 extrema, 1 path, 2 check)
+        const int cap = 100000;
+        while ((gmax > 0 || gmin > 0 || gdir > 0) && ite < cap) {
+            ++outer;
+            ite += 2;
+            while ((hmax > 0 || hmin > 0) && ite < cap) {
+                ++ite;
+                ++inner;
+                init_edits(r, d_edits);
+                zero_counters(r);
+                naive_iscriticle(r, dsm1, asm1, d_as, d_ds, d_in, d_dec, d_edits, d_cnt, d_or, d_flag, q, bound, delta,
+                                 ite, 0, 0, nx, ny);
+                read_counters(r, c);
+                hmax = c[0];
+                hmin = c[1];
+                recs.insert(recs.end(), {0u, c[0], c[1], 0u});
+            }
+            zero_counters(r);
+            path_compression(r, dsm1);
+            path_compression(r, asm1);
+            init_edits(r, d_edits);
+            false_path(r, d_dec, d_in, dsm, dsm1, asm0, asm1, d_or, d_ds, d_as, d_edits, d_cnt, q, bound, delta, ite,
+                       d_flag, 0);
+            read_counters(r, c);
+            recs.insert(recs.end(), {1u, 0u, 0u, c[2]});
+            naive_iscriticle(r, dsm1, asm1, d_as, d_ds, d_in, d_dec, d_edits, d_cnt, d_or, d_flag, q, bound, delta,
+                             ite, 0, 1, nx, ny);
+            zero_counters(r);
+            naive_iscriticle(r, dsm1, asm1, d_as, d_ds, d_in, d_dec, d_edits, d_cnt, d_or, d_flag, q, bound, delta,
+                             ite, 0, 1, nx, ny);
+            path_compression(r, dsm1);
+            path_compression(r, asm1);
+            false_path(r, d_dec, d_in, dsm, dsm1, asm0, asm1, d_or, d_ds, d_as, d_edits, d_cnt, q, bound, delta, ite,
+                       d_flag, 1);
+            read_counters(r, c);
+            recs.insert(recs.end(), {2u, c[0], c[1], c[2]});
+            hmax = gmax = c[0];
+            hmin = gmin = c[1];
+            gdir = c[2];
+        }
+        std::vector<double> field(r.N);
+        CK(cuMemcpyDtoH(field.data(), d_dec, r.N * 8));
+        write(out + "_field.bin", field.data(), r.N);
+        write(out + "_ite.bin", &ite, 1);
+        const int io[2] = {inner, outer};
+        write(out + "_passes.bin", io, 2);
+        write(out + "_recs.bin", recs.data(), recs.size());
         return 0;
     }
 

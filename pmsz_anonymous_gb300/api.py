@@ -62,10 +62,12 @@ class CorrectResult:
 
 
 def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
-            full_sweeps: bool = False, timing: bool = False, stream=None) -> CorrectResult:
+            full_sweeps: bool = False, timing: bool = False, stream=None, strategy: str = "pmsz") -> CorrectResult:
     """Correct fhat in place so that its extrema and both segmentations match f
-    (c_loops, pMSz.cu:1872-2074).  Raises PmszError except for
-    PMSZ_ERR_NOT_CONVERGED, which is reported in the result."""
+    (c_loops, pMSz.cu:1872-2074).  strategy="naive" runs the naive-MSz loop
+    instead (naive_MSz.cu:1887-2220; full_sweeps and timing do not apply).
+    Raises PmszError except for PMSZ_ERR_NOT_CONVERGED, which is reported in
+    the result."""
     _check_field(f, "f")
     _check_field(fhat, "fhat")
     if f.shape != fhat.shape or f.dtype != fhat.dtype or f.device != fhat.device:
@@ -77,7 +79,10 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
     nx, ny, nz = _dims(f)
     with torch.cuda.device(f.device):
-        st = getattr(L, f"pmsz_correct_{_suffix(f)}")(
+        if strategy not in ("pmsz", "naive"):
+            raise ValueError(f"unknown strategy {strategy!r}")
+        entry = "pmsz_correct_naive_" if strategy == "naive" else "pmsz_correct_"
+        st = getattr(L, entry + _suffix(f))(
             f.data_ptr(), fhat.data_ptr(), nx, ny, nz, float(eb), ctypes.byref(opts), ctypes.byref(res),
             _stream(stream))
     capi.check(st, allow=(capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED))
@@ -86,6 +91,51 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
                     dtype=np.uint64).reshape(n, len(SWEEP_KEYS))
     return CorrectResult(st, n, int(res.iteration), int(res.edits), rows, float(res.ms_first_pass),
                          float(res.ms_detect), float(res.ms_apply), int(res.launches), float(res.ms_total))
+
+
+def correct_host(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
+                 deltas: torch.Tensor | None = None, clamp: torch.Tensor | None = None,
+                 edits_only: bool = False, verify: bool = False, device=None, stream=None):
+    """pmsz_correct_host_*: the single-rank main pipeline on HOST tensors (pin
+    them for full copy bandwidth).  fhat is replaced by the corrected field
+    unless edits_only.  deltas (uint8, n) and clamp (field dtype, n) receive
+    the edit output when given.  Returns (CorrectResult, dict with n_clamp,
+    edit_count and, with verify, the verification counts)."""
+    for t, name in ((f, "f"), (fhat, "fhat")):
+        if t.device.type != "cpu" or not t.is_contiguous() or t.dtype not in (torch.float32, torch.float64):
+            raise ValueError(f"{name} must be a contiguous float32/float64 host tensor")
+    if f.shape != fhat.shape or f.dtype != fhat.dtype or f.dim() != 3:
+        raise ValueError("f and fhat must be 3-D host tensors of one shape and dtype")
+    n = f.numel()
+    if deltas is not None and (deltas.dtype != torch.uint8 or deltas.numel() < n or deltas.device.type != "cpu"):
+        raise ValueError("deltas must be a host uint8 tensor of n entries")
+    if clamp is not None and (clamp.dtype != f.dtype or clamp.numel() < n or clamp.device.type != "cpu"):
+        raise ValueError("clamp must be a host tensor of the field dtype with n entries")
+    L = capi.load()
+    flags = capi.PMSZ_FLAG_EDITS_ONLY if edits_only else 0
+    opts = capi.Opts(int(q), flags, int(max_sweeps))
+    log = (capi.SweepRecord * int(max_sweeps))()
+    res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
+    vres = capi.VerifyResult()
+    outs = capi.HostOutputs(deltas.data_ptr() if deltas is not None else None,
+                            clamp.data_ptr() if clamp is not None else None, 0, 0,
+                            ctypes.pointer(vres) if verify else None)
+    nz, ny, nx = f.shape
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    with torch.cuda.device(dev):
+        st = getattr(L, f"pmsz_correct_host_{_suffix(f)}")(
+            f.data_ptr(), fhat.data_ptr(), nx, ny, nz, float(eb), ctypes.byref(opts), ctypes.byref(res),
+            ctypes.byref(outs), _stream(stream))
+    capi.check(st, allow=(capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED))
+    k = int(res.sweeps)
+    rows = np.array([[getattr(log[i], key) for key in SWEEP_KEYS] for i in range(k)],
+                    dtype=np.uint64).reshape(k, len(SWEEP_KEYS))
+    extra = {"n_clamp": int(outs.n_clamp), "edit_count": int(outs.edit_count)}
+    if verify:
+        extra["verify"] = {name: int(getattr(vres, name)) for name, _ in capi.VerifyResult._fields_}
+    return (CorrectResult(st, k, int(res.iteration), int(res.edits), rows, float(res.ms_first_pass),
+                          float(res.ms_detect), float(res.ms_apply), int(res.launches), float(res.ms_total)),
+            extra)
 
 
 def codes(v: torch.Tensor, stream=None) -> torch.Tensor:

@@ -18,6 +18,8 @@ c_size, c_double, c_int, c_void_p = ctypes.c_size_t, ctypes.c_double, ctypes.c_i
 PMSZ_OK, PMSZ_ERR_ARG, PMSZ_ERR_OOM, PMSZ_ERR_NOT_CONVERGED, PMSZ_ERR_CUDA, PMSZ_ERR_IO = range(6)
 PMSZ_FLAG_FULL_SWEEPS = 1
 PMSZ_FLAG_TIMING = 2
+PMSZ_FLAG_EDITS_ONLY = 4
+PMSZ_FLAG_NAIVE = 8
 
 
 class Opts(ctypes.Structure):
@@ -65,6 +67,8 @@ _P = c_void_p
 SIGNATURES = {
     "pmsz_correct_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P]),
     "pmsz_correct_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P]),
+    "pmsz_correct_naive_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P]),
+    "pmsz_correct_naive_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P]),
     "pmsz_codes_f32": (c_int, [_P, c_size, c_size, c_size, _P, _P]),
     "pmsz_codes_f64": (c_int, [_P, c_size, c_size, c_size, _P, _P]),
     "pmsz_rank_offset": (c_int, [c_int, _P, _P, _P]),

@@ -41,7 +41,7 @@ struct Args {
     size_t W = 0, H = 0, D = 0;
     double eb = 0;
     int px = 1, py = 1, pz = 1;
-    bool f32 = false, full = false, verify = false;
+    bool f32 = false, full = false, verify = false, naive = false;
     int q = 5;
     long long max_sweeps = 10000;
     double cmp_size = 0;
@@ -52,7 +52,8 @@ int usage(const char *msg) {
                  "error: %s\nusage: pmsz <path>,<W>,<H>,<D> <abs_eb> <sz3|zfp> <PX> <PY> <PZ> [options]\n"
                  "       pmsz <path> <W> <H> <D> <abs_eb> <sz3|zfp> <PX> <PY> <PZ> [options]\n"
                  "options: --decp FILE  --dtype f64|f32  --q N  --max-sweeps N  --full-sweeps\n"
-                 "         --out FILE   --verify  --cmp-size BYTES\n",
+                 "         --out FILE   --verify  --cmp-size BYTES\n"
+                 "         --naive      the naive-MSz strategy (the reference's naive_MSz program)\n",
                  msg);
     return 2;
 }
@@ -83,6 +84,7 @@ int parse(int argc, char **argv, Args &a) {
         else if (s == "--cmp-size") { const char *v = need("n"); if (!v) return usage("--cmp-size needs a value"); a.cmp_size = std::atof(v); }
         else if (s == "--full-sweeps") a.full = true;
         else if (s == "--verify") a.verify = true;
+        else if (s == "--naive") a.naive = true;
         else if (s.size() > 2 && s[0] == '-' && s[1] == '-') return usage(("unknown option " + s).c_str());
         else pos.push_back(s);
     }
@@ -193,7 +195,7 @@ int run(const Args &a) {
     outs.deltas = deltas.data();
     outs.clamp = clamp.data();
     outs.verify = a.verify ? &vr : nullptr;
-    pmsz_opts opts{a.q, a.full ? PMSZ_FLAG_FULL_SWEEPS : 0u, a.max_sweeps};
+    pmsz_opts opts{a.q, (a.full ? PMSZ_FLAG_FULL_SWEEPS : 0u) | (a.naive ? PMSZ_FLAG_NAIVE : 0u), a.max_sweeps};
     pmsz_result res{};
     std::cout << "topology preserving started!" << std::endl;
     const auto t0 = std::chrono::steady_clock::now();

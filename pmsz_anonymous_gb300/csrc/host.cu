@@ -33,7 +33,8 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
     PMSZ_CUDA(cudaMemcpyAsync(dfh, fhat, n * sizeof(T), cudaMemcpyHostToDevice, s));
     if (want_edits) PMSZ_CUDA(cudaMemcpyAsync(dprev, dfh, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
-    const int st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
+    const int st = opts && (opts->flags & PMSZ_FLAG_NAIVE) ? naive_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s)
+                                                         : correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
     std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
     if (want_edits) {
@@ -45,7 +46,8 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
         if (outs->clamp && nc) PMSZ_CUDA(cudaMemcpyAsync(outs->clamp, dclamp, nc * sizeof(T), cudaMemcpyDeviceToHost, s));
     }
     if (want_verify && (rc = verify_impl<T>(df, dfh, nx, ny, nz, eb, outs->verify, s))) return rc;
-    PMSZ_CUDA(cudaMemcpyAsync(fhat, dfh, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    if (!(opts && (opts->flags & PMSZ_FLAG_EDITS_ONLY)))
+        PMSZ_CUDA(cudaMemcpyAsync(fhat, dfh, n * sizeof(T), cudaMemcpyDeviceToHost, s));
     PMSZ_CUDA(cudaStreamSynchronize(s));
     if ((rc = ws.release())) return rc;
     if (st == PMSZ_ERR_NOT_CONVERGED) set_error(st, keep);

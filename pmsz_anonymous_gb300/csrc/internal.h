@@ -95,6 +95,12 @@ int check_geom(size_t nx, size_t ny, size_t nz);
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
                  pmsz_result *res, cudaStream_t s);
+// AS / DS labels (roots of the steepest-ascent / descent forests) of a code
+// array; n < 2^32.
+int labels_impl(const uint8_t *codes, size_t nx, size_t ny, size_t nz, uint32_t *as, uint32_t *ds, cudaStream_t s);
+template <typename T>
+int naive_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
+               pmsz_result *res, cudaStream_t s);
 template <typename T>
 int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cudaStream_t s);
 template <typename T>

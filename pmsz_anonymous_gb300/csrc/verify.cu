@@ -2,7 +2,7 @@
 //
 // Replaces PathCompression (pMSz.cu:255-271): the reference walks every
 // vertex's pointer chain to its root one step at a time.  Here every round
-// replaces L[i] by L[L[i]] in place (a vertex's pointer only ever moves to
+// replaces L[i] by L[L[L[i]]] in place (a vertex's pointer only ever moves to
 // another vertex of its own chain, so concurrent readers see valid ancestors)
 // and the rounds stop when one changes nothing: O(log path length) rounds of
 // coalesced work instead of one unbounded walk per thread.

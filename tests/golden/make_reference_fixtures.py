@@ -12,9 +12,12 @@ writes one ``.npz`` per case:
 * ``correct_*`` the full reference loop on fields where every sweep edits a
                 single vertex (so the reference's in-place race cannot change
                 the result), plus three runs of the racy loop on a Perlin field;
-* ``extract_*`` extract_edits_kernel on (decompressed, oracle-corrected) pairs.
+* ``extract_*`` extract_edits_kernel on (decompressed, oracle-corrected) pairs;
+* ``naive_*``   the naive_MSz.cu loop (its own kernels, from
+                ``oracle/_ref/naive_ref.cubin``), three runs per field, with the
+                per-pass counts.
 
-Usage:  python tests/golden/make_reference_fixtures.py [outdir]
+Usage:  python tests/golden/make_reference_fixtures.py [outdir] [--only naive]
 (default outdir gpurun_out/reference_fixtures; the committed copies live in
 tests/golden/).
 """
@@ -52,6 +55,12 @@ def run(harness, cubin, mode, f, fh, eb, tmp, tag, cur=None):
         return np.fromfile(out + name, dtype=dt)
 
     res = {}
+    if mode == "naive":
+        res["field"] = load("_field.bin", np.float64).reshape(D, H, W)[1:-1, 1:-1, 1:-1].copy()
+        res["ite"] = load("_ite.bin", np.int32)
+        res["passes"] = load("_passes.bin", np.int32)
+        res["recs"] = load("_recs.bin", np.uint32).reshape(-1, 4)
+        return res
     if mode == "extract":
         res["deltas"] = load("_deltas.bin", np.uint8)
         res["editsout"] = load("_editsout.bin", np.float64)
@@ -67,8 +76,28 @@ def run(harness, cubin, mode, f, fh, eb, tmp, tag, cur=None):
     return res
 
 
+def naive_fixtures(harness, outdir, tmp):
+    if not os.path.exists(build_ref.NAIVE_CUBIN):
+        raise SystemExit("oracle/_ref/naive_ref.cubin is missing: build it where the reference sources exist")
+    cases = {}
+    f = F.perlin_field((20, 20, 20), 6, 4, 1 / 8, dtype=np.float64)
+    cases["perlin_zfp"] = (f, F.standin(f, 1e-3, "zfp", 6), 1e-3)
+    g = F.perlin_field((14, 16, 18), 7, 4, 1 / 8, dtype=np.float64)
+    cases["perlin_sz3"] = (g, F.standin(g, 2e-3, "sz3", 7), 2e-3)
+    for name, (f, fh, eb) in cases.items():
+        runs = [run(harness, build_ref.NAIVE_CUBIN, "naive", f, fh, eb, tmp, f"naive_{name}{k}") for k in range(3)]
+        np.savez_compressed(os.path.join(outdir, f"naive_{name}.npz"), f=f, fh=fh, eb=eb,
+                            fields=np.stack([r["field"] for r in runs]),
+                            ites=np.concatenate([r["ite"] for r in runs]),
+                            passes=runs[0]["passes"], recs=runs[0]["recs"])
+
+
 def main():
-    outdir = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "reference_fixtures")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only in args:
+        args.remove(only)
+    outdir = args[0] if args else os.path.join(ROOT, "gpurun_out", "reference_fixtures")
     os.makedirs(outdir, exist_ok=True)
     cubin = build_ref.build_cubin()
     if not cubin:
@@ -76,6 +105,10 @@ def main():
     harness = build_ref.build_harness()
     rng = np.random.default_rng(2024)
     tmp = tempfile.mkdtemp()
+    if only == "naive":
+        naive_fixtures(harness, outdir, tmp)
+        print("fixtures written to", outdir)
+        return
 
     label_cases = {}
     f = F.perlin_field((14, 16, 18), 3, 4, 1 / 8, dtype=np.float64)
@@ -123,6 +156,7 @@ def main():
         e = run(harness, cubin, "extract", f, fh, eb, tmp, name, cur=cur)
         np.savez_compressed(os.path.join(outdir, f"extract_{name}.npz"), f=f, fh=fh, cur=cur, eb=eb,
                             deltas=e["deltas"], editsout=e["editsout"], hcount=e["hcount"])
+    naive_fixtures(harness, outdir, tmp)
     print("fixtures written to", outdir)
 
 

@@ -224,3 +224,58 @@ def test_pack_nbits_round_trip_and_layout():
     assert len(packed) == 3
     np.testing.assert_array_equal(O.unpack_nbits(packed, sym.size, 3), sym)
     assert O.bits_for_max(5) == 3 and O.bits_for_max(0) == 1 and O.bits_for_max(7) == 3 and O.bits_for_max(8) == 4
+
+
+@pytest.mark.parametrize("comp", ["sz3", "zfp"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_naive_preserves_extrema_and_segmentations(comp, dtype):
+    """naive_MSz.cu's loop ends with no false extremum and no label mismatch,
+    and its last record is a clean check."""
+    eb = 1e-2
+    f, fh = _perlin_case((14, 12, 16), 7, dtype, comp, eb)
+    out, cnt, st, sw, recs = O.correct_naive(f, fh, eb)
+    assert st == O.OK
+    v = O.verify(f, out, eb)
+    assert v["ext_mismatch"] == 0
+    assert v["as_mismatch"] == 0 and v["ds_mismatch"] == 0
+    assert np.all(out <= fh)
+    assert np.all(out >= (f - dtype(eb)))
+    assert recs[-1].tolist() == [0, 0, 0, 0, 0]
+    # the first record is an extrema sweep: no direction count
+    assert recs[0][2] == 0
+
+
+def test_naive_record_sequence_structure():
+    """Extrema sweeps until one sees no false extremum, then a path repair
+    (no extremum counts) and a check (no edits)."""
+    eb = 1e-3
+    f, fh = _perlin_case((20, 18, 16), 8, np.float32, "zfp", eb)
+    out, cnt, st, sw, recs = O.correct_naive(f, fh, eb)
+    assert st == O.OK
+    prev, i = (1, 1), 0
+    while i < len(recs):
+        if prev[0] or prev[1]:
+            assert recs[i][2] == 0
+            prev = (recs[i][0], recs[i][1])
+            i += 1
+            continue
+        assert recs[i][0] == 0 and recs[i][1] == 0      # path repair
+        assert recs[i + 1][3] == 0 and recs[i + 1][4] == 0  # check
+        prev = (recs[i + 1][0], recs[i + 1][1])
+        i += 2
+    assert i == len(recs)
+
+
+def test_naive_is_thread_count_independent():
+    eb = 1e-3
+    f, fh = _perlin_case((24, 20, 18), 9, np.float64, "sz3", eb)
+    n0 = O.num_threads()
+    try:
+        O.set_threads(1)
+        a = O.correct_naive(f, fh, eb)
+        O.set_threads(max(2, n0))
+        b = O.correct_naive(f, fh, eb)
+    finally:
+        O.set_threads(n0)
+    assert a[0].tobytes() == b[0].tobytes()
+    np.testing.assert_array_equal(a[4], b[4])
