@@ -47,7 +47,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Gvox/s correction at 512³ fp64 vs ref 1-rank; batched vox/s; p50/p99 latency"
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
@@ -70,7 +70,7 @@ def parse():
     p.add_argument("--serve-jobs", type=int, default=120)
     p.add_argument("--serve-rates", default="100,300,1000,3000", help="arrival rates (jobs/s) to sweep")
     p.add_argument("--batch-fields", type=int, default=64)
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 class ClockSampler:
@@ -135,6 +135,25 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def max_over_ranks(value: float, device) -> float:
+    """Max of a per-rank scalar over the ranks of the default process group
+    (the value itself without one).  device is where the backend reduces:
+    the rank's GPU for NCCL, "cpu" for gloo."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(voxels_per_rank: int, world: int, ms: float) -> float:
+    """Gvox/s of the whole job: every rank corrects its own replica of
+    voxels_per_rank voxels, and the slowest rank's time ms bounds the job."""
+    return world * voxels_per_rank / (ms * 1e-3) / 1e9
 
 
 def profiled_traffic(name: str):
@@ -255,12 +274,8 @@ def run_ours(args):
                 raise RuntimeError(f"correction did not converge (status {r.status})")
         barrier()
         wall = time.perf_counter() - wall0
-    ms = statistics.mean(times)
-    if world > 1:
-        t = torch.tensor([ms], device=device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(statistics.mean(times), device)
+    value = whole_job_rate(n, world, ms)
 
     # e2e through the host-buffer C ABI (pmsz_correct_host_*): pinned host f and
     # fhat copied in, correction, edit extraction, and the reference main's
@@ -279,11 +294,7 @@ def run_ours(args):
         n_clamp = extra["n_clamp"]
         if i:
             e2e_times.append(start.elapsed_time(stop))
-    e2e_ms = statistics.mean(e2e_times) if e2e_times else float("nan")
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(statistics.mean(e2e_times) if e2e_times else float("nan"), device)
     if e2e_res is not None and (e2e_res.sweeps != last.sweeps or e2e_res.edits != last.edits):
         raise RuntimeError("host-buffer call disagrees with the device-buffer call")
     ok = api.verify(f, fh, args.eb)
@@ -303,7 +314,7 @@ def run_ours(args):
                                          "ms_detect_sparse": last.ms_detect, "ms_apply": last.ms_apply,
                                          "active_per_sweep": [int(v) for v in last.log[:, 6]],
                                          "requested_per_sweep": [int(v) for v in last.log[:, 3]]}),
-        "e2e": {"value": world * n / (e2e_ms * 1e-3) / 1e9, "unit": "Gvox/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": whole_job_rate(n, world, e2e_ms), "unit": "Gvox/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n + n_clamp * itemsize,
                 "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY: H2D f and fhat, correction, "
                         "edit extraction, D2H delta symbols (1 B/voxel) and clamp list"},

@@ -25,7 +25,8 @@
 // 2 per voxel), <out>_dir_as.bin / _dir_ds.bin (int32), <out>_counts.bin
 // (3 uint32: count_f_max / min / dir after the last pass), <out>_field.bin
 // (double), <out>_ite.bin (int32), <out>_deltas.bin (uint8, core, x fastest),
-// <out>_editsout.bin (double, core, before compaction), <out>_hcount.bin.
+// <out>_editsout.bin (double, core, before compaction), <out>_hcount.bin,
+// <out>_ms.bin (float: device-synchronised ms of the loop, correct / naive).
 #include <cuda.h>
 
 #include <cstdio>
@@ -151,6 +152,24 @@ void false_path(Ref &r, CUdeviceptr decp, CUdeviceptr input, CUdeviceptr dsm0, C
     CK(cuCtxSynchronize());
 }
 
+// Device-synchronised wall time of the loop, from the original labelling to
+// convergence (the window of the reference's "comfputational overhead" print).
+struct Clock {
+    CUevent a, b;
+    Clock() {
+        CK(cuEventCreate(&a, CU_EVENT_DEFAULT));
+        CK(cuEventCreate(&b, CU_EVENT_DEFAULT));
+    }
+    void start() { CK(cuEventRecord(a, 0)); }
+    float stop() {
+        CK(cuEventRecord(b, 0));
+        CK(cuEventSynchronize(b));
+        float ms = 0;
+        CK(cuEventElapsedTime(&ms, a, b));
+        return ms;
+    }
+};
+
 void init_edits(Ref &r, CUdeviceptr edits) {
     size_t ds = r.N;
     void *a[] = {&ds, &edits};
@@ -274,6 +293,8 @@ int main(int argc, char **argv) {
         CK(cuMemsetD32(asm0, 0, r.N));
         CK(cuMemsetD32(dsm1, 0, r.N));
         CK(cuMemsetD32(asm1, 0, r.N));
+        Clock clock;
+        clock.start();
         {
             size_t ds = r.N;
             void *args[] = {&ds, &d_cnt};
@@ -328,10 +349,12 @@ int main(int argc, char **argv) {
             hmin = gmin = c[1];
             gdir = c[2];
         }
+        const float ms = clock.stop();
         std::vector<double> field(r.N);
         CK(cuMemcpyDtoH(field.data(), d_dec, r.N * 8));
         write(out + "_field.bin", field.data(), r.N);
         write(out + "_ite.bin", &ite, 1);
+        write(out + "_ms.bin", &ms, 1);
         const int io[2] = {inner, outer};
         write(out + "_passes.bin", io, 2);
         write(out + "_recs.bin", recs.data(), recs.size());
@@ -339,6 +362,8 @@ int main(int argc, char **argv) {
     }
 
     // init_counter + original labelling (c_loops, pMSz.cu:1883-1895)
+    Clock clock;
+    clock.start();
     {
         size_t ds = r.N;
         void *args[] = {&ds, &d_cnt};
@@ -379,10 +404,12 @@ int main(int argc, char **argv) {
             gmin = c[1];
             gdir = c[2];
         }
+        const float ms = clock.stop();
         std::vector<double> field(r.N);
         CK(cuMemcpyDtoH(field.data(), d_dec, r.N * 8));
         write(out + "_field.bin", field.data(), r.N);
         write(out + "_ite.bin", &ite, 1);
+        write(out + "_ms.bin", &ms, 1);
     } else if (mode != "label") {
         std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
         return 2;

@@ -251,9 +251,57 @@ int check_geom(size_t nx, size_t ny, size_t nz) {
     return PMSZ_OK;
 }
 
+// The fused first pass over a field that is still being copied in from the
+// host: slabs of whole z-chunks (about 64 MiB of f + fhat each) go up on a
+// copy stream, each followed by an event; the first pass of a slab's chunks
+// waits for the next slab's event (its tiles read one plane beyond the slab).
+template <typename T>
+int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
+                      uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches) {
+    if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+    const int nchunks = (g.nz + kZChunk - 1) / kZChunk;
+    const size_t chunk_bytes = 2 * plane * kZChunk * sizeof(T);
+    const int cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
+    const int nslabs = (nchunks + cps - 1) / cps;
+    struct Res {
+        cudaStream_t cs = nullptr;
+        std::vector<cudaEvent_t> ev;
+        ~Res() {  // released once pending work completes
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } r;
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    r.ev.assign(static_cast<size_t>(nslabs) + 1, nullptr);
+    for (cudaEvent_t &e : r.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
+    PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
+    for (int j = 0; j < nslabs; ++j) {
+        const size_t z0 = static_cast<size_t>(j) * cps * kZChunk;
+        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * kZChunk);
+        const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
+        PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
+        PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
+        if (in.dprev) PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.cs));
+        PMSZ_CUDA(cudaEventRecord(r.ev[j], r.cs));
+    }
+    const dim3 blk3(kTX, kTY, 1);
+    for (int j = 0; j < nslabs; ++j) {
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
+        dim3 grid = tiled_grid(g);
+        grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
+        k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
+        PMSZ_CUDA(cudaGetLastError());
+        ++*launches;
+    }
+    return PMSZ_OK;
+}
+
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
-                 pmsz_result *res, cudaStream_t s) {
+                 pmsz_result *res, cudaStream_t s, const HostIngest<T> *ingest) {
     if (!f || !fh) return set_error(PMSZ_ERR_ARG, "null field pointer");
     int rc = check_geom(nx, ny, nz);
     if (rc) return rc;
@@ -307,10 +355,12 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         SweepSlot *slot = slots + sweeps;
         uint32_t *a_next = act[cur ^ 1];
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
-        if (sweeps == 0) {
-            k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g);
+        if (sweeps == 0 && ingest) {
+            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, a_next, slot, g, s, &launches))) return rc;
+        } else if (sweeps == 0) {
+            k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, 0);
         } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
-            k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g);
+            k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g, 0);
         } else {
             k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
         }
@@ -401,7 +451,7 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
     int rc = check_geom(nx, ny, nz);
     if (rc) return rc;
     const Geom g = make_geom(nx, ny, nz);
-    k_tiled<T, kCodes><<<tiled_grid(g), dim3(kTX, kTY, 1), 0, s>>>(v, nullptr, codes, nullptr, nullptr, nullptr, nullptr, g);
+    k_tiled<T, kCodes><<<tiled_grid(g), dim3(kTX, kTY, 1), 0, s>>>(v, nullptr, codes, nullptr, nullptr, nullptr, nullptr, g, 0);
     PMSZ_CUDA(cudaGetLastError());
     return PMSZ_OK;
 }
@@ -409,8 +459,8 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
 template int codes_impl<float>(const float *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
 template int codes_impl<double>(const double *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
 
-template int correct_impl<float>(const float *, float *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t);
-template int correct_impl<double>(const double *, double *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t);
+template int correct_impl<float>(const float *, float *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t, const HostIngest<float> *);
+template int correct_impl<double>(const double *, double *, size_t, size_t, size_t, double, const pmsz_opts *, pmsz_result *, cudaStream_t, const HostIngest<double> *);
 
 }  // namespace pmsz
 

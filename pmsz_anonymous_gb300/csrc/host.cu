@@ -30,11 +30,17 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     if (rc) return rc;
     T *df = ws.at<T>(o_f), *dfh = ws.at<T>(o_fh), *dprev = ws.at<T>(o_prev), *dclamp = ws.at<T>(o_c);
     uint8_t *dd = ws.at<uint8_t>(o_d);
-    PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
-    PMSZ_CUDA(cudaMemcpyAsync(dfh, fhat, n * sizeof(T), cudaMemcpyHostToDevice, s));
-    if (want_edits) PMSZ_CUDA(cudaMemcpyAsync(dprev, dfh, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
-    const int st = opts && (opts->flags & PMSZ_FLAG_NAIVE) ? naive_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s)
-                                                         : correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
+    int st;
+    if (opts && (opts->flags & PMSZ_FLAG_NAIVE)) {
+        PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
+        PMSZ_CUDA(cudaMemcpyAsync(dfh, fhat, n * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (want_edits) PMSZ_CUDA(cudaMemcpyAsync(dprev, dfh, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        st = naive_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
+    } else {
+        // the copies in overlap the fused first pass (slab by slab)
+        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr};
+        st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s, &in);
+    }
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
     std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
     if (want_edits) {

@@ -92,9 +92,19 @@ void *host_pinned(size_t bytes);
 // Implementations behind the C entry points (explicitly instantiated for
 // float and double in their translation units).
 int check_geom(size_t nx, size_t ny, size_t nz);
+// Host-resident inputs of pmsz_correct_host_*: f and fhat are copied in slab
+// by slab on a second stream while the fused first pass already runs on the
+// slabs that have arrived (the host link, not HBM, bounds that phase).
+// df / dfh are the device destinations (the f / fh of correct_impl); dprev,
+// if not null, receives a device copy of the input fhat.
+template <typename T>
+struct HostIngest {
+    const T *hf, *hfh;
+    T *df, *dprev;
+};
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
-                 pmsz_result *res, cudaStream_t s);
+                 pmsz_result *res, cudaStream_t s, const HostIngest<T> *ingest = nullptr);
 // AS / DS labels (roots of the steepest-ascent / descent forests) of a code
 // array; n < 2^32.
 int labels_impl(const uint8_t *codes, size_t nx, size_t ny, size_t nz, uint32_t *as, uint32_t *ds, cudaStream_t s);

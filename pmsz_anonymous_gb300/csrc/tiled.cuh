@@ -220,13 +220,16 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
     if (MODE != kCodes) flush_counts(slot, cmax, cmin, cdir, active, bad);
 }
 
+// bz0: index of the first z-chunk the launch covers (a launch may cover a
+// z-range of chunks, e.g. the part of the field already copied in).
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
                                                        uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
                                                        uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
-                                                       SweepSlot *slot, Geom g) {
+                                                       SweepSlot *slot, Geom g, int bz0) {
     __shared__ TileSmem<T, MODE == kFirst ? 2 : 1> sm;
-    tiled_body<T, MODE>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, blockIdx.z);
+    tiled_body<T, MODE>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y,
+                        bz0 + static_cast<int>(blockIdx.z));
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,130 @@
+"""Host-buffer entry points (pmsz_correct_host_*) and the drop-in CLI.
+
+The host call copies f and fhat in slab by slab while the first pass runs on
+the slabs already present; its result must equal the device-buffer call bit
+for bit, and its edit output must equal pmsz_extract_edits on the same pair.
+The CLI's _deltas.bin / _edits.bin must decode to the same edit output."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pmsz_anonymous_gb300 import _build, capi, fields as F
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def api():
+    from pmsz_anonymous_gb300 import api as A
+    return A
+
+
+HOST_CASES = [
+    ((256, 256, 256), torch.float32, "zfp", 1e-3, 31),   # several copy slabs, a short last one
+    ((70, 33, 45), torch.float64, "sz3", 2e-3, 32),      # nz not a multiple of the 32-plane chunk
+    ((5, 17, 33), torch.float32, "zfp", 5e-3, 33),
+    ((130, 96, 160), torch.float64, "zfp", 1e-4, 34),    # 5 chunks, 2 slabs of 64 MiB
+]
+
+
+@pytest.mark.parametrize("case", HOST_CASES, ids=lambda c: f"{c[0]}-{str(c[1])[6:]}-{c[2]}")
+def test_host_call_matches_device_call(cuda, case):
+    shape, dt, comp, eb, seed = case
+    A = api()
+    f = A.gen_perlin(shape, seed, 4, 1 / 16, dtype=dt, device=cuda)
+    fh = A.standin(f, eb, comp, seed)
+    ref = fh.clone()
+    r = A.correct(f, ref, eb)
+    d_ref, c_ref, ec_ref = A.extract_edits(fh, ref, f, eb)
+    n = f.numel()
+    hf, hfh = f.cpu().pin_memory(), fh.cpu().pin_memory()
+    deltas = torch.empty(n, dtype=torch.uint8).pin_memory()
+    clamp = torch.empty(n, dtype=dt).pin_memory()
+    for edits_only in (False, True):
+        work = hfh.clone().pin_memory()
+        rh, extra = A.correct_host(hf, work, eb, deltas=deltas, clamp=clamp, edits_only=edits_only, verify=True)
+        assert (rh.status, rh.sweeps, rh.edits) == (r.status, r.sweeps, r.edits)
+        np.testing.assert_array_equal(rh.log, r.log)
+        if edits_only:
+            assert torch.equal(work.view(torch.uint8), hfh.view(torch.uint8))
+        else:
+            assert torch.equal(work.view(torch.uint8), ref.cpu().view(torch.uint8))
+        assert torch.equal(deltas, d_ref.cpu().view(-1))
+        assert extra["n_clamp"] == c_ref.numel()
+        assert torch.equal(clamp[: extra["n_clamp"]].view(torch.uint8), c_ref.cpu().view(torch.uint8))
+        assert extra["edit_count"] == ec_ref
+        v = extra["verify"]
+        assert v["dir_mismatch"] == 0 and v["ext_mismatch"] == 0 and v["bound_beyond_clamp"] == 0
+
+
+def test_host_call_with_pageable_buffers_and_naive_flag(cuda):
+    """Pageable (not pinned) host arrays, both strategies, through the raw C
+    entry point with a NULL outputs pointer."""
+    shape, eb = (40, 36, 30), 1e-3
+    f = F.perlin_field(shape, 35, 4, 1 / 16, dtype=np.float32)
+    fh = F.standin(f, eb, "sz3", 35)
+    L = capi.load()
+    nz, ny, nx = shape
+    for flags, ref_fn in ((0, O.correct), (capi.PMSZ_FLAG_NAIVE, O.correct_naive)):
+        ref = ref_fn(f, fh, eb)[0]
+        work = fh.copy()
+        opts, res = capi.Opts(5, flags, 10000), capi.Result()
+        st = L.pmsz_correct_host_f32(f.ctypes.data, work.ctypes.data, nx, ny, nz, eb, ctypes.byref(opts),
+                                     ctypes.byref(res), None, None)
+        assert st == capi.PMSZ_OK
+        np.testing.assert_array_equal(work.view(np.uint8), ref.view(np.uint8))
+
+
+def _cli():
+    _build.build()
+    exe = os.path.join(os.path.dirname(_build.__file__), "lib", "pmsz")
+    assert os.path.exists(exe), "the pmsz CLI was not built"
+    return exe
+
+
+@pytest.mark.parametrize("naive", [False, True])
+def test_cli_outputs_decode_to_the_edit_output(cuda, tmp_path, naive):
+    exe = _cli()
+    shape, eb = (24, 20, 28), 1e-3
+    f = F.perlin_field(shape, 36, 4, 1 / 16, dtype=np.float64)
+    fh = F.standin(f, eb, "zfp", 36)
+    (tmp_path / "stat_result").mkdir()
+    path, decp, out = tmp_path / "field.bin", tmp_path / "decp.bin", tmp_path / "corrected.bin"
+    f.tofile(path)
+    fh.tofile(decp)
+    nz, ny, nx = shape
+    cmd = [exe, f"{path},{nx},{ny},{nz}", repr(eb), "zfp", "1", "1", "1", "--decp", str(decp), "--out", str(out),
+           "--verify"] + (["--naive"] if naive else [])
+    p = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    for key in ("iteration is:", "Edit count:", "comfputational overhead is:", "overall edit ratio is:"):
+        assert key in p.stdout
+    ref, cnt, st, sw, recs = (O.correct_naive if naive else O.correct)(f, fh, eb)
+    got = np.fromfile(out, np.float64).reshape(shape)
+    np.testing.assert_array_equal(got.view(np.uint8), ref.view(np.uint8))
+    deltas, clamp, ec = O.extract_edits(fh, ref, f, eb)
+    A = api()
+    blob_d = (tmp_path / "_deltas.bin").read_bytes()
+    blob_e = (tmp_path / "_edits.bin").read_bytes()
+    np.testing.assert_array_equal(A.decode_deltas(blob_d, f.size), deltas)
+    np.testing.assert_array_equal(A.decode_clamps(blob_e, np.float64).view(np.uint8), clamp.view(np.uint8))
+    assert blob_d == A.encode_deltas(deltas) and blob_e == A.encode_clamps(clamp)
+    assert f"Edit count: {ec}" in p.stdout
+    assert (tmp_path / "stat_result").iterdir()
+
+
+def test_cli_rejects_multi_rank_grids_and_bad_arguments(tmp_path):
+    exe = _cli()
+    p = subprocess.run([exe, "x.bin,4,4,4", "1e-3", "sz3", "2", "1", "1"], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=60)
+    assert p.returncode != 0 and "PX PY PZ" in p.stderr
+    p = subprocess.run([exe, "x.bin,4,4", "1e-3", "sz3", "1", "1", "1"], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=60)
+    assert p.returncode != 0
+    p = subprocess.run([exe, str(tmp_path / "missing.bin") + ",4,4,4", "1e-3", "sz3", "1", "1", "1"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert p.returncode != 0
