@@ -264,18 +264,25 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
     const size_t chunk_bytes = 2 * plane * kZChunk * sizeof(T);
     const int cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
     const int nslabs = (nchunks + cps - 1) / cps;
+    // cs: host copies; ds: device copies of fhat into dprev (kept off cs so
+    // the host link never idles behind them)
     struct Res {
-        cudaStream_t cs = nullptr;
+        cudaStream_t cs = nullptr, ds = nullptr;
         std::vector<cudaEvent_t> ev;
+        cudaEvent_t done = nullptr;
         ~Res() {  // released once pending work completes
             for (cudaEvent_t e : ev)
                 if (e) cudaEventDestroy(e);
+            if (done) cudaEventDestroy(done);
             if (cs) cudaStreamDestroy(cs);
+            if (ds) cudaStreamDestroy(ds);
         }
     } r;
     PMSZ_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.ds, cudaStreamNonBlocking));
     r.ev.assign(static_cast<size_t>(nslabs) + 1, nullptr);
     for (cudaEvent_t &e : r.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PMSZ_CUDA(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
     PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
     PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
     for (int j = 0; j < nslabs; ++j) {
@@ -284,9 +291,13 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
         const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
         PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
         PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
-        if (in.dprev) PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.cs));
         PMSZ_CUDA(cudaEventRecord(r.ev[j], r.cs));
+        if (in.dprev) {
+            PMSZ_CUDA(cudaStreamWaitEvent(r.ds, r.ev[j], 0));
+            PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.ds));
+        }
     }
+    PMSZ_CUDA(cudaEventRecord(r.done, in.dprev ? r.ds : r.cs));
     const dim3 blk3(kTX, kTY, 1);
     for (int j = 0; j < nslabs; ++j) {
         PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
@@ -296,6 +307,7 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
         PMSZ_CUDA(cudaGetLastError());
         ++*launches;
     }
+    PMSZ_CUDA(cudaStreamWaitEvent(s, r.done, 0));  // dprev complete before the first edit
     return PMSZ_OK;
 }
 
@@ -317,7 +329,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     // Scratch: codes (n), counters (n), request + two active bitmaps, sweep slots.
     Workspace ws(s);
     const size_t o_codes = ws.reserve<uint8_t>(g.n);
-    const size_t o_cnt = ws.reserve<uint8_t>(g.n);
+    const bool own_cnt = !(ingest && ingest->cnt);
+    const size_t o_cnt = ws.reserve<uint8_t>(own_cnt ? g.n : 0);
     const size_t o_req = ws.reserve<uint32_t>(g.nwords);
     const size_t o_a0 = ws.reserve<uint32_t>(g.nwords);
     const size_t o_a1 = ws.reserve<uint32_t>(g.nwords);
@@ -326,7 +339,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
-    uint8_t *cnt = ws.at<uint8_t>(o_cnt);
+    uint8_t *cnt = own_cnt ? ws.at<uint8_t>(o_cnt) : ingest->cnt;
     uint32_t *req = ws.at<uint32_t>(o_req);
     uint32_t *act[2] = {ws.at<uint32_t>(o_a0), ws.at<uint32_t>(o_a1)};
     SweepSlot *slots = ws.at<SweepSlot>(o_slots);

@@ -26,10 +26,12 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     const size_t o_prev = ws.reserve<T>(want_edits ? n : 0);
     const size_t o_d = ws.reserve<uint8_t>(want_edits ? n : 0);
     const size_t o_c = ws.reserve<T>(want_edits ? n : 0);
+    const size_t o_cnt = ws.reserve<uint8_t>(want_edits ? n : 0);
     int rc = ws.commit();
     if (rc) return rc;
     T *df = ws.at<T>(o_f), *dfh = ws.at<T>(o_fh), *dprev = ws.at<T>(o_prev), *dclamp = ws.at<T>(o_c);
     uint8_t *dd = ws.at<uint8_t>(o_d);
+    uint8_t *dcnt = want_edits ? ws.at<uint8_t>(o_cnt) : nullptr;
     int st;
     if (opts && (opts->flags & PMSZ_FLAG_NAIVE)) {
         PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
@@ -38,14 +40,16 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
         st = naive_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
     } else {
         // the copies in overlap the fused first pass (slab by slab)
-        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr};
+        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr, dcnt};
         st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s, &in);
     }
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
     std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
     if (want_edits) {
         uint64_t nc = 0, ec = 0;
-        if ((rc = extract_impl<T>(dprev, dfh, df, n, eb, q, dd, dclamp, &nc, &ec, s))) return rc;
+        const bool counted = !(opts && (opts->flags & PMSZ_FLAG_NAIVE));  // the pMSz loop left its counters in dcnt
+        if ((rc = extract_impl<T>(dprev, dfh, df, n, eb, q, dd, dclamp, &nc, &ec, s, counted ? dcnt : nullptr)))
+            return rc;
         outs->n_clamp = nc;
         outs->edit_count = ec;
         if (outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));

@@ -95,12 +95,15 @@ int check_geom(size_t nx, size_t ny, size_t nz);
 // Host-resident inputs of pmsz_correct_host_*: f and fhat are copied in slab
 // by slab on a second stream while the fused first pass already runs on the
 // slabs that have arrived (the host link, not HBM, bounds that phase).
-// df / dfh are the device destinations (the f / fh of correct_impl); dprev,
-// if not null, receives a device copy of the input fhat.
+// df is the device destination of f (the f of correct_impl; fhat goes to its
+// fh); dprev, if not null, receives a device copy of the input fhat; cnt, if
+// not null, is a caller buffer of n bytes the correction uses as its edit
+// counters (left holding them for the edit extraction).
 template <typename T>
 struct HostIngest {
     const T *hf, *hfh;
     T *df, *dprev;
+    uint8_t *cnt;
 };
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
@@ -116,8 +119,10 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
 template <typename T>
 int verify_impl(const T *f, const T *fp, size_t nx, size_t ny, size_t nz, double eb, pmsz_verify_result *out,
                 cudaStream_t s);
+// cnt (optional): edit counters of the correction that turned prev into cur;
+// voxels with counter 0 are then known unchanged and not read.
 template <typename T>
 int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas, T *clamp,
-                 uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s);
+                 uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s, const uint8_t *cnt = nullptr);
 
 }  // namespace pmsz
