@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) k_codes(const T *__restrict__ v, uint8_t 
 
 }  // namespace pmsz
 
-#include "tiled.cuh"
+#include "list.cuh"
 
 namespace pmsz {
 
@@ -336,6 +336,10 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const size_t o_a1 = ws.reserve<uint32_t>(g.nwords);
     const size_t o_slots = ws.reserve<SweepSlot>(static_cast<size_t>(max_sweeps));
     const size_t o_hp = ws.reserve<uint32_t>(g.n);
+    // voxel-list sweeps (list.cuh) for fields of fewer than 2^32 voxels
+    const bool use_list = !(flags & PMSZ_FLAG_FULL_SWEEPS) && g.n < (static_cast<size_t>(1) << 32);
+    const size_t o_list = ws.reserve<uint32_t>(use_list ? g.n : 0);
+    const size_t o_lcnt = ws.reserve<uint32_t>(use_list ? 2 * static_cast<size_t>(max_sweeps) : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
@@ -343,6 +347,10 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint32_t *req = ws.at<uint32_t>(o_req);
     uint32_t *act[2] = {ws.at<uint32_t>(o_a0), ws.at<uint32_t>(o_a1)};
     SweepSlot *slots = ws.at<SweepSlot>(o_slots);
+    uint32_t *list = use_list ? ws.at<uint32_t>(o_list) : nullptr;
+    uint32_t *lcnt = use_list ? ws.at<uint32_t>(o_lcnt) : nullptr;  // two list lengths per sweep
+    const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
+    const unsigned list_blocks = 152 * 8;
     EventTimer et;
     if ((rc = et.init())) return rc;
     PMSZ_CUDA(cudaEventRecord(et.ev[3], s));  // start of the loop's device window
@@ -352,6 +360,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
+    if (use_list) PMSZ_CUDA(cudaMemsetAsync(lcnt, 0, 2 * sizeof(uint32_t) * static_cast<size_t>(max_sweeps), s));
 
     SweepSlot *hslot = static_cast<SweepSlot *>(host_pinned(sizeof(SweepSlot)));
     if (!hslot) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
@@ -372,15 +381,30 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, a_next, slot, g, s, &launches))) return rc;
         } else if (sweeps == 0) {
             k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, 0);
+            ++launches;
         } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
             k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g, 0);
+            ++launches;
+        } else if (use_list) {
+            uint32_t *lc = lcnt + 2 * sweeps;
+            k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(act[cur], g, list, lc);
+            k_detect_list<T><<<list_blocks, 256, 0, s>>>(list, lc, fh, hp, codes, req, a_next, slot, g, div_nx);
+            launches += 2;
         } else {
             k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
+            ++launches;
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
-        k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
+        if (use_list) {
+            uint32_t *lc = lcnt + 2 * sweeps + 1;
+            k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(req, g, list, lc);
+            k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, lc, f, fh, cnt, hp, a_next, slot, g, div_nx, eps, delta, q);
+            launches += 2;
+        } else {
+            k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
+            ++launches;
+        }
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[2], s));
-        launches += 2;
         PMSZ_CUDA(cudaGetLastError());
         PMSZ_CUDA(cudaMemcpyAsync(hslot, slot, sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
         PMSZ_CUDA(cudaStreamSynchronize(s));
