@@ -339,7 +339,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     // voxel-list sweeps (list.cuh) for fields of fewer than 2^32 voxels
     const bool use_list = !(flags & PMSZ_FLAG_FULL_SWEEPS) && g.n < (static_cast<size_t>(1) << 32);
     const size_t o_list = ws.reserve<uint32_t>(use_list ? g.n : 0);
-    const size_t o_lcnt = ws.reserve<uint32_t>(use_list ? 2 * static_cast<size_t>(max_sweeps) : 0);
+    const size_t o_xlist = ws.reserve<uint32_t>(use_list ? g.n : 0);
+    const size_t o_lcnt = ws.reserve<uint32_t>(use_list ? 3 * static_cast<size_t>(max_sweeps) : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
@@ -348,7 +349,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint32_t *act[2] = {ws.at<uint32_t>(o_a0), ws.at<uint32_t>(o_a1)};
     SweepSlot *slots = ws.at<SweepSlot>(o_slots);
     uint32_t *list = use_list ? ws.at<uint32_t>(o_list) : nullptr;
-    uint32_t *lcnt = use_list ? ws.at<uint32_t>(o_lcnt) : nullptr;  // two list lengths per sweep
+    uint32_t *xlist = use_list ? ws.at<uint32_t>(o_xlist) : nullptr;
+    uint32_t *lcnt = use_list ? ws.at<uint32_t>(o_lcnt) : nullptr;  // three list lengths per sweep
     const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
     const unsigned list_blocks = 152 * 8;
     EventTimer et;
@@ -360,7 +362,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
-    if (use_list) PMSZ_CUDA(cudaMemsetAsync(lcnt, 0, 2 * sizeof(uint32_t) * static_cast<size_t>(max_sweeps), s));
+    if (use_list) PMSZ_CUDA(cudaMemsetAsync(lcnt, 0, 3 * sizeof(uint32_t) * static_cast<size_t>(max_sweeps), s));
 
     SweepSlot *hslot = static_cast<SweepSlot *>(host_pinned(sizeof(SweepSlot)));
     if (!hslot) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
@@ -386,17 +388,19 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g, 0);
             ++launches;
         } else if (use_list) {
-            uint32_t *lc = lcnt + 2 * sweeps;
+            uint32_t *lc = lcnt + 3 * sweeps;
             k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(act[cur], g, list, lc);
-            k_detect_list<T><<<list_blocks, 256, 0, s>>>(list, lc, fh, hp, codes, req, a_next, slot, g, div_nx);
-            launches += 2;
+            k_detect_list<T><<<list_blocks, 256, 0, s>>>(list, lc, hp, codes, req, a_next, xlist, lc + 2, slot, g,
+                                                         div_nx);
+            k_detect_exact<T><<<list_blocks, 256, 0, s>>>(xlist, lc + 2, fh, codes, req, a_next, slot, g, div_nx);
+            launches += 3;
         } else {
             k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
             ++launches;
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
         if (use_list) {
-            uint32_t *lc = lcnt + 2 * sweeps + 1;
+            uint32_t *lc = lcnt + 3 * sweeps + 1;
             k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(req, g, list, lc);
             k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, lc, f, fh, cnt, hp, a_next, slot, g, div_nx, eps, delta, q);
             launches += 2;

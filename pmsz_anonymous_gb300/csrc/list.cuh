@@ -10,7 +10,9 @@
 //                   the list order is arbitrary -- every consumer is
 //                   order-free (requests and marks are bit ORs, counters sums)
 //   k_detect_list   one thread per listed voxel: the 15 proxies, the rules,
-//                   the requests, the mismatch bit of the next active set
+//                   the requests, the mismatch bit of the next active set;
+//                   failed certificates go to a second list
+//   k_detect_exact  the second list on full keys
 //   k_compact       request bitmap -> list
 //   k_apply_list    one thread per requested voxel: the edit, the proxy
 //                   refresh, the closed-stencil marks of the next active set
@@ -90,15 +92,33 @@ __device__ __forceinline__ void voxel_coords(const Geom &g, const FastDiv &div_n
     z = static_cast<int>(zz);
 }
 
-// Detection of every listed voxel (iscriticle data_type=0 on the proxy array,
-// exact keys on a failed certificate); a mismatch sets the voxel's bit of the
-// next active set.
+// Outcome of one voxel's steepest ranks: the rules, the requests and the
+// mismatch bit of the next active set.
+__device__ __forceinline__ void detect_outcome(const Geom &g, int x, int y, int z, int asc, int desc, uint8_t c,
+                                               uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                               uint32_t &cmax, uint32_t &cmin, uint32_t &cdir) {
+    const uint32_t tm = detect_rules(asc, desc, c & 15, c >> 4, cmax, cmin, cdir);
+    if (tm) {
+        request_targets(req, g, x, y, z, tm);
+        atomicOr(act_next + word_of(g, x, y, z), 1u << (x & 31));
+    }
+}
+
+// Detection of every listed voxel (iscriticle data_type=0) on the proxy
+// array.  A voxel whose certificate fails (ties in the truncated proxies) is
+// appended to a second list and decided by k_detect_exact on full keys, so
+// this loop never runs a one-lane slow path.
+constexpr uint32_t kExactCap = 2048;  // failed certificates buffered per block
 template <typename T>
-__global__ void __launch_bounds__(256, 4) k_detect_list(const uint32_t *__restrict__ list, const uint32_t *count,
-                                                     const T *__restrict__ fh, const uint32_t *__restrict__ hp,
-                                                     const uint8_t *__restrict__ codes, uint32_t *__restrict__ req,
-                                                     uint32_t *__restrict__ act_next, SweepSlot *slot, Geom g,
-                                                     FastDiv div_nx) {
+__global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restrict__ list, const uint32_t *count,
+                                                     const uint32_t *__restrict__ hp, const uint8_t *__restrict__ codes,
+                                                     uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                     uint32_t *__restrict__ exact_list, uint32_t *exact_count,
+                                                     SweepSlot *slot, Geom g, FastDiv div_nx) {
+    __shared__ uint32_t s_exact[kExactCap];
+    __shared__ uint32_t s_n, s_base;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
     const uint32_t m = *count;
     uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
     const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
@@ -116,25 +136,51 @@ __global__ void __launch_bounds__(256, 4) k_detect_list(const uint32_t *__restri
             t[r] = ((valid >> r) & 1u) ? __ldg(c0 + off) : 0u;
         }
         const uint8_t c = __ldg(codes + i);
-        Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
-        if (!ex.exact) {  // ties in the truncated proxies: the 15 exact keys, loaded together
-            using K = typename KeyOf<T>::type;
-            K kk[15];
-#pragma unroll
-            for (int r = 0; r < 15; ++r) {
-                const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
-                kk[r] = ((valid >> r) & 1u) ? okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off))) : K(0);
-            }
-            arg_ext(kk, valid, ex.asc, ex.desc);
-        }
-        const uint32_t tm = detect_rules(ex.asc, ex.desc, c & 15, c >> 4, cmax, cmin, cdir);
+        const Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
         ++active;
-        if (tm) {
-            request_targets(req, g, x, y, z, tm);
-            atomicOr(act_next + word_of(g, x, y, z), 1u << (x & 31));
+        if (ex.exact) {
+            detect_outcome(g, x, y, z, ex.asc, ex.desc, c, req, act_next, cmax, cmin, cdir);
+        } else {  // buffered in shared memory; a full buffer spills straight to the list
+            const uint32_t pos = atomicAdd(&s_n, 1u);
+            if (pos < kExactCap) s_exact[pos] = i;
+            else exact_list[atomicAdd(exact_count, 1u)] = i;
         }
     }
     flush_counts(slot, cmax, cmin, cdir, active, 0);
+    __syncthreads();
+    const uint32_t nb = min(s_n, kExactCap);
+    if (threadIdx.x == 0) s_base = nb ? atomicAdd(exact_count, nb) : 0u;  // one global atomic per block
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) exact_list[s_base + j] = s_exact[j];
+}
+
+// The voxels whose certificate failed: steepest ranks on the 15 exact keys of
+// fhat (loaded together), then the same outcome.
+template <typename T>
+__global__ void __launch_bounds__(256) k_detect_exact(const uint32_t *__restrict__ exact_list, const uint32_t *count,
+                                                      const T *__restrict__ fh, const uint8_t *__restrict__ codes,
+                                                      uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                      SweepSlot *slot, Geom g, FastDiv div_nx) {
+    const uint32_t m = *count;
+    uint32_t cmax = 0, cmin = 0, cdir = 0;
+    const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(exact_list + k);
+        int x, y, z;
+        voxel_coords(g, div_nx, i, x, y, z);
+        const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        using K = typename KeyOf<T>::type;
+        K kk[15];
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+            kk[r] = ((valid >> r) & 1u) ? okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off))) : K(0);
+        }
+        int asc, desc;
+        arg_ext(kk, valid, asc, desc);
+        detect_outcome(g, x, y, z, asc, desc, __ldg(codes + i), req, act_next, cmax, cmin, cdir);
+    }
+    flush_counts(slot, cmax, cmin, cdir, 0, 0);
 }
 
 // The edit of every listed voxel (applyDeltaBuffer_local, pMSz.cu:623-645),
