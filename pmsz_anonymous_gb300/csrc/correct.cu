@@ -341,6 +341,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const size_t o_list = ws.reserve<uint32_t>(use_list ? g.n : 0);
     const size_t o_xlist = ws.reserve<uint32_t>(use_list ? g.n : 0);
     const size_t o_lcnt = ws.reserve<uint32_t>(use_list ? 3 * static_cast<size_t>(max_sweeps) : 0);
+    const size_t o_bcnt = ws.reserve<uint32_t>(use_list ? kCompactBlocks : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
@@ -351,6 +352,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint32_t *list = use_list ? ws.at<uint32_t>(o_list) : nullptr;
     uint32_t *xlist = use_list ? ws.at<uint32_t>(o_xlist) : nullptr;
     uint32_t *lcnt = use_list ? ws.at<uint32_t>(o_lcnt) : nullptr;  // three list lengths per sweep
+    uint32_t *bcnt = use_list ? ws.at<uint32_t>(o_bcnt) : nullptr;  // per-block counts of a compaction
     const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
     const unsigned list_blocks = 152 * 8;
     EventTimer et;
@@ -389,11 +391,11 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             ++launches;
         } else if (use_list) {
             uint32_t *lc = lcnt + 3 * sweeps;
-            k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(act[cur], g, list, lc);
+            compact_bitmap(act[cur], g, bcnt, list, lc, s);
             k_detect_list<T><<<list_blocks, 256, 0, s>>>(list, lc, hp, codes, req, a_next, xlist, lc + 2, slot, g,
                                                          div_nx);
             k_detect_exact<T><<<list_blocks, 256, 0, s>>>(xlist, lc + 2, fh, codes, req, a_next, slot, g, div_nx);
-            launches += 3;
+            launches += 4;
         } else {
             k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
             ++launches;
@@ -401,9 +403,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
         if (use_list) {
             uint32_t *lc = lcnt + 3 * sweeps + 1;
-            k_compact<<<compact_grid(g), kCompactBlock, 0, s>>>(req, g, list, lc);
+            compact_bitmap(req, g, bcnt, list, lc, s);
             k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, lc, f, fh, cnt, hp, a_next, slot, g, div_nx, eps, delta, q);
-            launches += 2;
+            launches += 3;
         } else {
             k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
             ++launches;

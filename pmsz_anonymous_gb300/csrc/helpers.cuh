@@ -47,6 +47,28 @@ __device__ __forceinline__ void flush_counts(SweepSlot *slot, uint32_t cmax, uin
     }
 }
 
+// Adds per-thread counters to the 8 fields of a sweep slot (fmax, fmin, fdir,
+// requested, changed, progressed, active, bad) with one atomic per non-zero
+// field per BLOCK: thousands of warps adding to the same few addresses
+// serialise at L2.  Every thread of the block must call it.
+__device__ __forceinline__ void block_flush_slot(SweepSlot *slot, const uint32_t (&v)[8]) {
+    __shared__ uint32_t s_red[8][32];
+    const int nwarps = (blockDim.x * blockDim.y + 31) >> 5;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int w = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t sum = warp_sum_u32(v[c]);
+        if ((tid & 31) == 0) s_red[c][w] = sum;
+    }
+    __syncthreads();
+    if (tid < 8) {
+        unsigned long long total = 0;
+        for (int k = 0; k < nwarps; ++k) total += s_red[tid][k];
+        if (total) atomicAdd(reinterpret_cast<unsigned long long *>(slot) + tid, total);
+    }
+}
+
 __device__ __forceinline__ void or_word(uint32_t *act, const Geom &g, int wx, int y, int z, uint32_t m) {
     if (!m || wx < 0 || wx >= g.wpr || y < 0 || y >= g.ny || z < 0 || z >= g.nz) return;
     m &= row_tail_mask(g, wx);

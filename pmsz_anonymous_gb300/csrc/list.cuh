@@ -5,15 +5,14 @@
 // of compacting and processing a bitmap round by round inside one kernel
 // (which keeps the round state and the detection registers live together and
 // caps residency at a few blocks per SM), each sweep runs as
-//   k_compact       bitmap -> list of flat voxel indices (clears the bitmap);
-//                   one atomicAdd per block claims its slice of the list, so
-//                   the list order is arbitrary -- every consumer is
-//                   order-free (requests and marks are bit ORs, counters sums)
+//   compaction      bitmap -> list of flat voxel indices in voxel order
+//                   (clears the bitmap); every consumer is order-free anyway
+//                   (requests and marks are bit ORs, counters sums)
 //   k_detect_list   one thread per listed voxel: the 15 proxies, the rules,
 //                   the requests, the mismatch bit of the next active set;
 //                   failed certificates go to a second list
 //   k_detect_exact  the second list on full keys
-//   k_compact       request bitmap -> list
+//   compaction      request bitmap -> list
 //   k_apply_list    one thread per requested voxel: the edit, the proxy
 //                   refresh, the closed-stencil marks of the next active set
 // The per-voxel kernels are light enough for full residency, so the 15
@@ -27,25 +26,76 @@ namespace pmsz {
 constexpr int kCompactBlock = 256;
 constexpr int kCompactWords = kCompactBlock * 4;  // one uint4 of words per thread per step
 
-// Bitmap -> list.  list[*count ...] receives nx-flat voxel indices.
-__global__ void __launch_bounds__(kCompactBlock) k_compact(uint32_t *__restrict__ bm, Geom g,
-                                                           uint32_t *__restrict__ list, uint32_t *count) {
+// Bitmap -> list in two passes with a deterministic order and no contended
+// atomics: k_count_words sums the set bits of each block's contiguous range of
+// words; k_write_list derives its block's offset from the counts before it,
+// writes the flat indices of its range in order and clears the words.  Block b
+// of both kernels covers words [b * per, (b + 1) * per), per a multiple of 4.
+constexpr int kCompactBlocks = 152 * 8;
+
+__host__ __device__ __forceinline__ size_t compact_per(const Geom &g) {
+    return ((g.nwords + kCompactBlocks - 1) / kCompactBlocks + 3) & ~static_cast<size_t>(3);
+}
+
+__device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t *s_warp) {
+    const int t = threadIdx.x;
+    v = warp_sum_u32(v);
+    if ((t & 31) == 0) s_warp[t >> 5] = v;
+    __syncthreads();
+    uint32_t tot = 0;
+    for (int k = 0; k < kCompactBlock / 32; ++k) tot += s_warp[k];
+    __syncthreads();
+    return tot;
+}
+
+__global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *__restrict__ bm, Geom g,
+                                                               uint32_t *__restrict__ counts) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
-    __shared__ uint32_t s_base;
+    const size_t per = compact_per(g);
+    const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(g.nwords, lo + per);
+    uint32_t c = 0;
+    for (size_t w0 = lo + static_cast<size_t>(threadIdx.x) * 4; w0 < hi; w0 += kCompactWords) {
+        if (w0 + 4 <= hi) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(bm + w0);
+            c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+        } else {
+            for (size_t w = w0; w < hi; ++w) c += __popc(bm[w]);
+        }
+    }
+    c = block_sum_u32(c, s_warp);
+    if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
+                                                              const uint32_t *__restrict__ counts,
+                                                              uint32_t *__restrict__ list, uint32_t *total) {
+    __shared__ uint32_t s_warp[kCompactBlock / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    for (size_t base = static_cast<size_t>(blockIdx.x) * kCompactWords; base < g.nwords;
-         base += static_cast<size_t>(gridDim.x) * kCompactWords) {
+    uint32_t before = 0, all = 0;
+    for (int b = t; b < static_cast<int>(gridDim.x); b += kCompactBlock) {
+        const uint32_t c = counts[b];
+        all += c;
+        if (b < static_cast<int>(blockIdx.x)) before += c;
+    }
+    uint32_t pos = block_sum_u32(before, s_warp);
+    all = block_sum_u32(all, s_warp);
+    if (blockIdx.x == 0 && t == 0) *total = all;
+    const size_t per = compact_per(g);
+    const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(g.nwords, lo + per);
+    for (size_t base = lo; base < hi; base += kCompactWords) {
         const size_t w0 = base + static_cast<size_t>(t) * 4;
-        uint32_t w[4];
-        if (w0 + 4 <= g.nwords) {
+        uint32_t w[4] = {0u, 0u, 0u, 0u};
+        if (w0 + 4 <= hi) {
             const uint4 v = *reinterpret_cast<const uint4 *>(bm + w0);
             w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
             if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4 *>(bm + w0) = make_uint4(0, 0, 0, 0);
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                w[j] = w0 + j < g.nwords ? bm[w0 + j] : 0u;
-                if (w[j]) bm[w0 + j] = 0;
+                if (w0 + j < hi) {
+                    w[j] = bm[w0 + j];
+                    if (w[j]) bm[w0 + j] = 0;
+                }
             }
         }
         const uint32_t c = __popc(w[0]) + __popc(w[1]) + __popc(w[2]) + __popc(w[3]);
@@ -57,18 +107,15 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(uint32_t *__restrict_
         }
         if (lane == 31) s_warp[warp] = inc;
         __syncthreads();
-        if (t == 0) {
-            uint32_t run = 0;
-            for (int k = 0; k < kCompactBlock / 32; ++k) {
-                const uint32_t v = s_warp[k];
-                s_warp[k] = run;
-                run += v;
-            }
-            s_base = run ? atomicAdd(count, run) : 0u;
+        uint32_t wbase = 0, step = 0;
+        for (int k = 0; k < kCompactBlock / 32; ++k) {
+            const uint32_t v = s_warp[k];
+            if (k < warp) wbase += v;
+            step += v;
         }
-        __syncthreads();
+        __syncthreads();  // s_warp is rewritten by the next step
         if (c) {
-            uint32_t pos = s_base + s_warp[warp] + inc - c;
+            uint32_t p = pos + wbase + inc - c;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (!w[j]) continue;
@@ -76,10 +123,10 @@ __global__ void __launch_bounds__(kCompactBlock) k_compact(uint32_t *__restrict_
                 const uint32_t row = fdiv(wj, g.div_wpr);
                 const uint32_t wx = wj - row * static_cast<uint32_t>(g.wpr);
                 const uint32_t i0 = row * static_cast<uint32_t>(g.nx) + (wx << 5);
-                for (uint32_t bits = w[j]; bits; bits &= bits - 1) list[pos++] = i0 + static_cast<uint32_t>(__ffs(bits) - 1);
+                for (uint32_t bits = w[j]; bits; bits &= bits - 1) list[p++] = i0 + static_cast<uint32_t>(__ffs(bits) - 1);
             }
         }
-        __syncthreads();  // s_warp / s_base are rewritten by the next step
+        pos += step;
     }
 }
 
@@ -146,8 +193,8 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
             else exact_list[atomicAdd(exact_count, 1u)] = i;
         }
     }
-    flush_counts(slot, cmax, cmin, cdir, active, 0);
-    __syncthreads();
+    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, 0u};
+    block_flush_slot(slot, v);  // ends with a barrier: s_n is final
     const uint32_t nb = min(s_n, kExactCap);
     if (threadIdx.x == 0) s_base = nb ? atomicAdd(exact_count, nb) : 0u;  // one global atomic per block
     __syncthreads();
@@ -180,7 +227,8 @@ __global__ void __launch_bounds__(256) k_detect_exact(const uint32_t *__restrict
         arg_ext(kk, valid, asc, desc);
         detect_outcome(g, x, y, z, asc, desc, __ldg(codes + i), req, act_next, cmax, cmin, cdir);
     }
-    flush_counts(slot, cmax, cmin, cdir, 0, 0);
+    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, 0u, 0u};
+    block_flush_slot(slot, v);
 }
 
 // The edit of every listed voxel (applyDeltaBuffer_local, pMSz.cu:623-645),
@@ -222,12 +270,16 @@ __global__ void __launch_bounds__(256) k_apply_list(const uint32_t *__restrict__
             mark_stencil(act_next, g, x >> 5, y, z, 1u << (x & 31));
         }
     }
-    flush_apply_counts(slot, nreq, nchg, nprog);
+    const uint32_t v[8] = {0u, 0u, 0u, nreq, nchg, nprog, 0u, 0u};
+    block_flush_slot(slot, v);
 }
 
-inline unsigned compact_grid(const Geom &g) {
-    const size_t need = (g.nwords + kCompactWords - 1) / kCompactWords;
-    return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(need, 152 * 8)));
+// Bitmap -> list (k_count_words, k_write_list); counts: kCompactBlocks words of
+// scratch; *total receives the list length.
+inline void compact_bitmap(uint32_t *bm, const Geom &g, uint32_t *counts, uint32_t *list, uint32_t *total,
+                           cudaStream_t s) {
+    k_count_words<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts);
+    k_write_list<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts, list, total);
 }
 
 }  // namespace pmsz

@@ -217,7 +217,10 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
         }
         __syncthreads();
     }
-    if (MODE != kCodes) flush_counts(slot, cmax, cmin, cdir, active, bad);
+    if (MODE != kCodes) {
+        const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, bad};
+        block_flush_slot(slot, v);
+    }
 }
 
 // bz0: index of the first z-chunk the launch covers (a launch may cover a
@@ -420,8 +423,9 @@ struct DetectWork {
         if (tm) request_targets(req, g, x, y, z, tm);
         return tm != 0;
     }
-    __device__ __forceinline__ void flush_to(SweepSlot *slot) {
-        flush_counts(slot, cmax, cmin, cdir, active, 0);
+    __device__ __forceinline__ void flush_to(SweepSlot *slot) {  // every thread of the block
+        const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, 0u};
+        block_flush_slot(slot, v);
         cmax = cmin = cdir = active = 0;
     }
 };
@@ -516,7 +520,8 @@ __device__ __forceinline__ void apply_body(ListSmem &sm, const T *__restrict__ f
     ApplyWork<L, T> work{f, fh, cnt, hp, g, eps, delta, q};
     ApplyFlush flush{act_next, g};
     for_each_set_bit<L>(sm, req, g, work, flush);
-    flush_apply_counts(slot, work.nreq, flush.nchg, work.nprog);
+    const uint32_t v[8] = {0u, 0u, 0u, work.nreq, flush.nchg, work.nprog, 0u, 0u};
+    block_flush_slot(slot, v);
 }
 
 template <typename T>
