@@ -66,10 +66,15 @@ __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *_
     if (threadIdx.x == 0) counts[blockIdx.x] = c;
 }
 
+// Four words per thread per step (one 16-byte load); the step's first
+// kStage entries are staged in shared memory in order and copied out with
+// coalesced stores, any beyond (only in very dense steps) go out directly.
+constexpr uint32_t kStage = 8192;
 __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
                                                               const uint32_t *__restrict__ counts,
                                                               uint32_t *__restrict__ list, uint32_t *total) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
+    __shared__ uint32_t s_stage[kStage];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t before = 0, all = 0;
     for (int b = t; b < static_cast<int>(gridDim.x); b += kCompactBlock) {
@@ -113,9 +118,8 @@ __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restri
             if (k < warp) wbase += v;
             step += v;
         }
-        __syncthreads();  // s_warp is rewritten by the next step
         if (c) {
-            uint32_t p = pos + wbase + inc - c;
+            uint32_t p = wbase + inc - c;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (!w[j]) continue;
@@ -123,10 +127,18 @@ __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restri
                 const uint32_t row = fdiv(wj, g.div_wpr);
                 const uint32_t wx = wj - row * static_cast<uint32_t>(g.wpr);
                 const uint32_t i0 = row * static_cast<uint32_t>(g.nx) + (wx << 5);
-                for (uint32_t bits = w[j]; bits; bits &= bits - 1) list[p++] = i0 + static_cast<uint32_t>(__ffs(bits) - 1);
+                for (uint32_t bits = w[j]; bits; bits &= bits - 1, ++p) {
+                    const uint32_t e = i0 + static_cast<uint32_t>(__ffs(bits) - 1);
+                    if (p < kStage) s_stage[p] = e;
+                    else list[pos + p] = e;
+                }
             }
         }
+        __syncthreads();
+        const uint32_t staged = min(step, kStage);
+        for (uint32_t e = t; e < staged; e += kCompactBlock) list[pos + e] = s_stage[e];
         pos += step;
+        __syncthreads();  // s_warp / s_stage are rewritten by the next step
     }
 }
 
