@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) k_codes(const T *__restrict__ v, uint8_t 
 
 }  // namespace pmsz
 
-#include "list.cuh"
+#include "tail.cuh"
 
 namespace pmsz {
 
@@ -207,20 +207,28 @@ static int run_sweep_loop(const T *f, T *fh, const uint8_t *codes, uint8_t *cnt,
     PMSZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PMSZ_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return set_error(PMSZ_ERR_CUDA, "device does not support cooperative launches");
-    PMSZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_loop<T>, kListBlock, 0));
+    PMSZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tail_loop<T>, kTailBlock, 0));
     if (per_sm < 1) return set_error(PMSZ_ERR_CUDA, "sweep loop kernel does not fit on an SM");
-    const size_t need = (g.nwords + kRoundWords - 1) / kRoundWords;
-    const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(need, static_cast<size_t>(per_sm) * sms)));
+    const size_t ns = summary_words(g);
+    const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(ns, static_cast<size_t>(per_sm) * sms)));
     long long *d_done = nullptr;
     Workspace ws(s);
     const size_t o_done = ws.reserve<long long>(1);
+    const size_t o_sum = ws.reserve<uint32_t>(3 * ns);
     int rc = ws.commit();
     if (rc) return rc;
     d_done = ws.at<long long>(o_done);
-    LoopArgs<T> a{f, fh, codes, cnt, hp, req, act[0], act[1], slots, first, max_sweeps, d_done, g, eps, delta, q};
-    void *args[] = {&a};
+    uint32_t *sum = ws.at<uint32_t>(o_sum);  // summaries of act[0], act[1], req
     if (et) PMSZ_CUDA(cudaEventRecord(et->ev[0], s));
-    PMSZ_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k_sweep_loop<T>), dim3(grid), dim3(kListBlock),
+    PMSZ_CUDA(cudaMemsetAsync(sum, 0, 3 * ns * sizeof(uint32_t), s));
+    const int c = static_cast<int>(first & 1);
+    k_build_summary<<<static_cast<unsigned>(std::min<size_t>((ns + 7) / 8, 152 * 16)), 256, 0, s>>>(
+        act[c], g, sum + static_cast<size_t>(c) * ns);
+    PMSZ_CUDA(cudaGetLastError());
+    TailArgs<T> a{f,    fh,        codes, cnt, hp,    req, act[0], act[1], sum + 2 * ns, sum, sum + ns,
+                  slots, first, max_sweeps, d_done, g,  eps, delta,  q};
+    void *args[] = {&a};
+    PMSZ_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k_tail_loop<T>), dim3(grid), dim3(kTailBlock),
                                           args, 0, s));
     if (et) PMSZ_CUDA(cudaEventRecord(et->ev[1], s));
     long long h = 0;
