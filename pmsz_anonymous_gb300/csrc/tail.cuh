@@ -14,8 +14,9 @@
 namespace pmsz {
 
 constexpr int kTailBlock = 256;
-constexpr int kSumChunk = 64;             // summary words staged per block step
-constexpr int kGroupCap = kSumChunk * 32;  // marked words of one summary step
+constexpr int kSumPerThread = 8;                       // summary words per thread and step
+constexpr int kSumStep = kTailBlock * kSumPerThread;   // 2048 summary words = 65536 bitmap words
+constexpr uint32_t kGroupCap = 2048;                   // marked words staged per pass
 
 __host__ __device__ __forceinline__ size_t summary_words(const Geom &g) { return (g.nwords + 31) / 32; }
 
@@ -86,8 +87,8 @@ struct TailSmem {
 };
 
 // Visits every set bit of a two-level bitmap (bm, sum), clearing both.  Block b
-// owns summary words [b * per, (b + 1) * per), staged kSumChunk at a time into
-// a list of marked words.  Those are taken 256 at a time (one per thread):
+// owns summary words [b * per, (b + 1) * per), read kSumStep at a time (an
+// empty step costs one barrier) and ranked into a list of marked words.  Those are taken 256 at a time (one per thread):
 // their set bits are ranked by a block scan into a shared list that all
 // threads share (visit(x, y, z) returns the voxel's result bit), and
 // flush(w, results) runs once per word by its owner thread.
@@ -120,52 +121,68 @@ __device__ __forceinline__ void for_each_set_bit_2l(TailSmem &sm, uint32_t *__re
     const size_t ns = summary_words(g);
     const size_t per = (ns + gridDim.x - 1) / gridDim.x;
     const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(ns, lo + per);
-    for (size_t base = lo; base < hi; base += kSumChunk) {
-        const size_t si = base + static_cast<size_t>(t);
-        uint32_t sw = 0;
-        if (t < kSumChunk && si < hi) {
-            sw = __ldcg(sum + si);
-            if (sw) sum[si] = 0;
+    for (size_t base = lo; base < hi; base += kSumStep) {
+        // kSumPerThread summary words per thread; an empty step costs one barrier
+        uint32_t sw[kSumPerThread];
+        uint32_t c = 0;
+#pragma unroll
+        for (int j = 0; j < kSumPerThread; ++j) {
+            const size_t si = base + static_cast<size_t>(t) * kSumPerThread + j;
+            sw[j] = si < hi ? __ldcg(sum + si) : 0u;
+            if (sw[j]) sum[si] = 0;
+            c += __popc(sw[j]);
         }
+        if (!__syncthreads_or(c != 0)) continue;
         uint32_t first;
-        const uint32_t ng = block_scan(__popc(sw), first);
-        for (uint32_t bits = sw; bits; bits &= bits - 1)
-            sm.groups[first++] = static_cast<uint32_t>(si * 32 + static_cast<size_t>(__ffs(bits) - 1));
-        __syncthreads();
-        // the marked words, 256 per step
-        for (uint32_t g0 = 0; g0 < ng; g0 += kTailBlock) {
-            const uint32_t gi = g0 + static_cast<uint32_t>(t);
-            size_t w = 0;
-            uint32_t m = 0;
-            if (gi < ng) {
-                w = sm.groups[gi];
-                m = __ldcg(bm + w);
-                if (m) bm[w] = 0;
+        const uint32_t nmarked = block_scan(c, first);
+        for (uint32_t lo1 = 0; lo1 < nmarked; lo1 += kGroupCap) {  // marked words, kGroupCap per pass
+            const uint32_t hi1 = lo1 + kGroupCap;
+            uint32_t r = first;
+#pragma unroll
+            for (int j = 0; j < kSumPerThread; ++j) {
+                const size_t si = base + static_cast<size_t>(t) * kSumPerThread + j;
+                for (uint32_t bits = sw[j]; bits; bits &= bits - 1, ++r)
+                    if (r >= lo1 && r < hi1)
+                        sm.groups[r - lo1] = static_cast<uint32_t>(si * 32 + static_cast<size_t>(__ffs(bits) - 1));
             }
-            sm.mask[t] = 0;
-            uint32_t rank;
-            const uint32_t total = block_scan(__popc(m), rank);
-            for (uint32_t lo2 = 0; lo2 < total; lo2 += kTailListCap) {
-                const uint32_t hi2 = lo2 + kTailListCap;
-                uint32_t r = rank;
-                for (uint32_t bits = m; bits; bits &= bits - 1, ++r)
-                    if (r >= lo2 && r < hi2) sm.list[r - lo2] = (static_cast<uint32_t>(t) << 5) | static_cast<uint32_t>(__ffs(bits) - 1);
-                __syncthreads();
-                const uint32_t n = min(kTailListCap, total - lo2);
-                for (uint32_t k = t; k < n; k += kTailBlock) {
-                    const uint32_t e = sm.list[k];
-                    const uint32_t slot = e >> 5;
-                    const int b = static_cast<int>(e & 31u);
-                    const size_t ww = sm.groups[g0 + slot];
-                    int wx, y, z;
-                    word_coords(g, ww, wx, y, z);
-                    if (visit(wx * 32 + b, y, z)) atomicOr(&sm.mask[slot], 1u << b);
+            __syncthreads();
+            const uint32_t ng = min(kGroupCap, nmarked - lo1);
+            // the marked words, 256 per step
+            for (uint32_t g0 = 0; g0 < ng; g0 += kTailBlock) {
+                const uint32_t gi = g0 + static_cast<uint32_t>(t);
+                size_t w = 0;
+                uint32_t m = 0;
+                if (gi < ng) {
+                    w = sm.groups[gi];
+                    m = __ldcg(bm + w);
+                    if (m) bm[w] = 0;
                 }
-                __syncthreads();
+                sm.mask[t] = 0;
+                uint32_t rank;
+                const uint32_t total = block_scan(__popc(m), rank);
+                for (uint32_t lo2 = 0; lo2 < total; lo2 += kTailListCap) {
+                    const uint32_t hi2 = lo2 + kTailListCap;
+                    uint32_t rr = rank;
+                    for (uint32_t bits = m; bits; bits &= bits - 1, ++rr)
+                        if (rr >= lo2 && rr < hi2)
+                            sm.list[rr - lo2] = (static_cast<uint32_t>(t) << 5) | static_cast<uint32_t>(__ffs(bits) - 1);
+                    __syncthreads();
+                    const uint32_t n = min(kTailListCap, total - lo2);
+                    for (uint32_t k = t; k < n; k += kTailBlock) {
+                        const uint32_t e = sm.list[k];
+                        const uint32_t slot = e >> 5;
+                        const int b = static_cast<int>(e & 31u);
+                        const size_t ww = sm.groups[g0 + slot];
+                        int wx, y, z;
+                        word_coords(g, ww, wx, y, z);
+                        if (visit(wx * 32 + b, y, z)) atomicOr(&sm.mask[slot], 1u << b);
+                    }
+                    __syncthreads();
+                }
+                const uint32_t res = sm.mask[t];
+                if (m && res) flush(w, res);
+                __syncthreads();  // mask / list are rewritten by the next step
             }
-            const uint32_t res = sm.mask[t];
-            if (m && res) flush(w, res);
-            __syncthreads();  // mask / list are rewritten by the next step
         }
     }
 }
