@@ -196,8 +196,9 @@ static inline unsigned stride_grid(size_t items) {
     return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(want, 152 * 16)));
 }
 
-// Runs sweeps first.. in one cooperative launch of k_sweep_loop (grid = the
-// number of co-resident blocks); *done receives the total number of sweeps.
+// Runs sweeps first.. in one cooperative launch of k_tail_loop (grid = the
+// number of co-resident blocks) after summarising the active bitmap of sweep
+// `first`; *done receives the total number of sweeps.
 template <typename T>
 static int run_sweep_loop(const T *f, T *fh, const uint8_t *codes, uint8_t *cnt, uint32_t *hp, uint32_t *req,
                           uint32_t *const act[2], SweepSlot *slots, int64_t first, int64_t max_sweeps, const Geom &g,

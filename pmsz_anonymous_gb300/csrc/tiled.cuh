@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa,
 
 // ---------------------------------------------------------------------------
 // Load policies.  Standalone sweep kernels read arrays that no thread of the
-// same launch writes through the read-only path (__ldg).  The persistent loop
-// kernel writes those arrays in one phase and reads them in the next, across
-// grid-wide barriers, so it reads them at L2 (__ldcg), never from a
-// possibly stale L1 line.
+// same launch writes through the read-only path (__ldg).  Persistent loop
+// kernels (the multi-field loop of batch.cu) write those arrays in one phase
+// and read them in the next, across grid-wide barriers, so they read them at
+// L2 (__ldcg), never from a possibly stale L1 line.
 // ---------------------------------------------------------------------------
 struct LdgLoads {
     template <class P>
@@ -548,50 +548,6 @@ __host__ __device__ __forceinline__ bool sweep_stops(unsigned long long fmax, un
                                                      unsigned long long fdir, unsigned long long progressed,
                                                      int64_t sweeps_done, int64_t max_sweeps) {
     return (fmax == 0 && fmin == 0 && fdir == 0) || progressed == 0 || sweeps_done >= max_sweeps;
-}
-
-template <typename T>
-struct LoopArgs {
-    const T *f;
-    T *fh;
-    const uint8_t *codes;
-    uint8_t *cnt;
-    uint32_t *hp, *req, *act0, *act1;
-    SweepSlot *slots;
-    int64_t first;       // index of the first sweep this launch runs
-    int64_t max_sweeps;
-    long long *sweeps_out;
-    Geom g;
-    T eps, delta;
-    int q;
-};
-
-// ---------------------------------------------------------------------------
-// The remaining sweeps of the loop in one cooperative launch: detect, grid
-// barrier, apply, grid barrier, then every thread reads the sweep's counters
-// and takes the same stop decision, so all blocks leave together.  Sweep k
-// reads act[k & 1] and fills act[(k + 1) & 1].  The loop is bounded by
-// max_sweeps.
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(kListBlock, 2) k_sweep_loop(LoopArgs<T> a) {
-    __shared__ ListSmem sm;
-    cg::grid_group grid = cg::this_grid();
-    int64_t k = a.first;
-    while (true) {
-        const SweepSlot *p = a.slots + (k - 1);
-        if (sweep_stops(__ldcg(&p->fmax), __ldcg(&p->fmin), __ldcg(&p->fdir), __ldcg(&p->progressed), k,
-                        a.max_sweeps))
-            break;
-        uint32_t *cur = (k & 1) ? a.act1 : a.act0;
-        uint32_t *nxt = (k & 1) ? a.act0 : a.act1;
-        sparse_detect_body<CgLoads>(sm, a.fh, a.hp, a.codes, cur, nxt, a.req, a.slots + k, a.g);
-        grid.sync();
-        apply_body<CgLoads>(sm, a.f, a.fh, a.cnt, a.hp, a.req, nxt, a.slots + k, a.g, a.eps, a.delta, a.q);
-        grid.sync();
-        ++k;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.sweeps_out = k;
 }
 
 inline dim3 tiled_grid(const Geom &g) {
