@@ -74,7 +74,9 @@ typedef struct pmsz_result {
     int64_t sweep_log_cap;
     /* With PMSZ_FLAG_TIMING (else 0): device milliseconds of the fused
      * labelling + first detection pass, of all later detection passes, and of
-     * all edit passes; launches = kernels launched by the call. */
+     * all edit passes (sweeps that run inside the device-side sweep loop count
+     * whole, edits included, as detection time); launches = kernels launched
+     * by the call. */
     double ms_first_pass, ms_detect, ms_apply;
     int64_t launches;
     /* Device milliseconds from the first to the last kernel of the loop

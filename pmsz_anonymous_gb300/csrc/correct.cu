@@ -349,8 +349,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const bool use_list = !(flags & PMSZ_FLAG_FULL_SWEEPS) && g.n < (static_cast<size_t>(1) << 32);
     const size_t o_list = ws.reserve<uint32_t>(use_list ? g.n : 0);
     const size_t o_xlist = ws.reserve<uint32_t>(use_list ? g.n : 0);
-    const size_t o_lcnt = ws.reserve<uint32_t>(use_list ? 3 * static_cast<size_t>(max_sweeps) : 0);
     const size_t o_bcnt = ws.reserve<uint32_t>(use_list ? kCompactBlocks : 0);
+    const size_t o_ls = ws.reserve<LoopState>(use_list ? 1 : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
@@ -360,8 +360,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     SweepSlot *slots = ws.at<SweepSlot>(o_slots);
     uint32_t *list = use_list ? ws.at<uint32_t>(o_list) : nullptr;
     uint32_t *xlist = use_list ? ws.at<uint32_t>(o_xlist) : nullptr;
-    uint32_t *lcnt = use_list ? ws.at<uint32_t>(o_lcnt) : nullptr;  // three list lengths per sweep
     uint32_t *bcnt = use_list ? ws.at<uint32_t>(o_bcnt) : nullptr;  // per-block counts of a compaction
+    LoopState *ls = use_list ? ws.at<LoopState>(o_ls) : nullptr;
     const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
     const unsigned list_blocks = 152 * 8;
     EventTimer et;
@@ -373,7 +373,10 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
-    if (use_list) PMSZ_CUDA(cudaMemsetAsync(lcnt, 0, 3 * sizeof(uint32_t) * static_cast<size_t>(max_sweeps), s));
+    if (use_list) {
+        PMSZ_CUDA(cudaMemsetAsync(ls, 0, sizeof(LoopState), s));
+        PMSZ_CUDA(cudaMemsetAsync(&ls->go, 1, 1, s));  // sweep 0 runs (little-endian int 1)
+    }
 
     SweepSlot *hslot = static_cast<SweepSlot *>(host_pinned(sizeof(SweepSlot)));
     if (!hslot) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
@@ -386,7 +389,129 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint64_t edits = 0;
     int status = PMSZ_ERR_NOT_CONVERGED;
     std::vector<SweepSlot> log;
-    while (sweeps < max_sweeps) {
+    const unsigned long long tail_at = std::max<unsigned long long>(g.n / 32, 1ull << 16);
+    if (use_list) {
+        // Sweep 0 (the fused first pass and its edits) on the stream; then the
+        // voxel-list sweeps as a CUDA graph whose while node repeats a body of
+        // two sweeps (odd: act[1] -> act[0], even: act[0] -> act[1]) for as
+        // long as k_loop_gate lets the next sweep run: no host round trip
+        // between sweeps.  The graph is built on the host while sweep 0 runs.
+        // What the gate leaves (a small active set) goes to the cooperative
+        // tail.
+        EventTimer lt;  // sweep 0 start, first pass done, sweep 0 done, list sweeps done
+        if (timing) {
+            if ((rc = lt.init())) return rc;
+            PMSZ_CUDA(cudaEventRecord(lt.ev[0], s));
+        }
+        if (ingest) {
+            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches)))
+                return rc;
+        } else {
+            k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act[1], &ls->cur, g, 0);
+            ++launches;
+        }
+        if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[1], s));
+        compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, s);
+        k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, act[1], &ls->cur, g, div_nx, eps,
+                                                    delta, q, &ls->go);
+        k_loop_gate<<<1, 32, 0, s>>>(ls, slots, max_sweeps, tail_at, cudaGraphConditionalHandle{}, 0);
+        launches += 4;
+        PMSZ_CUDA(cudaGetLastError());
+        if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
+
+        struct GraphGuard {
+            cudaGraph_t graph = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            cudaStream_t cs = nullptr;
+            ~GraphGuard() {
+                if (exec) cudaGraphExecDestroy(exec);
+                if (graph) cudaGraphDestroy(graph);
+                if (cs) cudaStreamDestroy(cs);
+            }
+        } gg;
+        PMSZ_CUDA(cudaGraphCreate(&gg.graph, 0));
+        cudaGraphConditionalHandle cond;
+        PMSZ_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t wnode;
+        PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        PMSZ_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
+        PMSZ_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        for (int half = 0; half < 2; ++half) {
+            uint32_t *a_cur = act[half == 0 ? 1 : 0], *a_next = act[half == 0 ? 0 : 1];
+            compact_bitmap(a_cur, g, bcnt, list, &ls->lc[0], &ls->go, gg.cs);
+            k_detect_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[0], hp, codes, req, a_next, xlist,
+                                                             &ls->lc[2], &ls->cur, g, div_nx, &ls->go);
+            k_detect_exact<T><<<list_blocks, 256, 0, gg.cs>>>(xlist, &ls->lc[2], fh, codes, req, a_next, &ls->cur, g,
+                                                              div_nx, &ls->go);
+            compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, gg.cs);
+            k_apply_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[1], f, fh, cnt, hp, a_next, &ls->cur, g,
+                                                            div_nx, eps, delta, q, &ls->go);
+            k_loop_gate<<<1, 32, 0, gg.cs>>>(ls, slots, max_sweeps, tail_at, cond, half);
+        }
+        PMSZ_CUDA(cudaStreamEndCapture(gg.cs, &body));
+        PMSZ_CUDA(cudaGraphInstantiate(&gg.exec, gg.graph, 0));
+        PMSZ_CUDA(cudaGraphLaunch(gg.exec, s));
+        if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[3], s));
+
+        LoopState *hls = static_cast<LoopState *>(host_pinned(sizeof(LoopState)));
+        if (!hls) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+        PMSZ_CUDA(cudaMemcpyAsync(hls, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
+        const int64_t nloop = std::max<int64_t>(done - 1, 0);
+        launches += 16 * std::max<int64_t>(1, (nloop + 1) / 2);
+        if (timing) {  // the list sweeps' edits run inside the graph and count as detection time
+            float a = 0, b = 0, c = 0;
+            PMSZ_CUDA(cudaEventElapsedTime(&a, lt.ev[0], lt.ev[1]));
+            PMSZ_CUDA(cudaEventElapsedTime(&b, lt.ev[1], lt.ev[2]));
+            PMSZ_CUDA(cudaEventElapsedTime(&c, lt.ev[2], lt.ev[3]));
+            ms_first += a;
+            ms_apply += b;
+            ms_detect += c;
+        }
+        log.resize(static_cast<size_t>(done));
+        PMSZ_CUDA(cudaMemcpyAsync(log.data(), slots, static_cast<size_t>(done) * sizeof(SweepSlot),
+                                  cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        for (const SweepSlot &t : log) edits += t.requested;
+        sweeps = done;
+        const SweepSlot h = log.back();
+        if (sweeps == 1 && h.bad) {
+            status = set_error(PMSZ_ERR_ARG, "input contains NaN or the value 1e30 (the reference's halo sentinel)");
+        } else if (h.fmax == 0 && h.fmin == 0 && h.fdir == 0) {
+            status = PMSZ_OK;
+        } else if (h.progressed == 0) {
+            set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
+        } else if (sweeps < max_sweeps) {  // the gate handed the rest to the cooperative tail
+            int64_t done2 = 0;
+            if ((rc = run_sweep_loop<T>(f, fh, codes, cnt, hp, req, act, slots, sweeps, max_sweeps, g, eps, delta, q,
+                                        s, timing ? &et : nullptr, &ms_detect, &done2)))
+                return rc;
+            ++launches;
+            const size_t m = static_cast<size_t>(done2 - sweeps);
+            if (m) {
+                std::vector<SweepSlot> tail(m);
+                PMSZ_CUDA(cudaMemcpyAsync(tail.data(), slots + sweeps, m * sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
+                PMSZ_CUDA(cudaStreamSynchronize(s));
+                for (const SweepSlot &t : tail) {
+                    log.push_back(t);
+                    edits += t.requested;
+                }
+                const SweepSlot &last = tail.back();
+                if (last.fmax == 0 && last.fmin == 0 && last.fdir == 0) status = PMSZ_OK;
+                else if (last.progressed == 0)
+                    set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
+            }
+            sweeps = done2;
+        }
+    }
+    while (!use_list && sweeps < max_sweeps) {
         SweepSlot *slot = slots + sweeps;
         uint32_t *a_next = act[cur ^ 1];
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
@@ -398,27 +523,13 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         } else if (flags & PMSZ_FLAG_FULL_SWEEPS) {
             k_tiled<T, kDetect><<<tiled_grid(g), blk3, 0, s>>>(fh, nullptr, codes, nullptr, req, a_next, slot, g, 0);
             ++launches;
-        } else if (use_list) {
-            uint32_t *lc = lcnt + 3 * sweeps;
-            compact_bitmap(act[cur], g, bcnt, list, lc, s);
-            k_detect_list<T><<<list_blocks, 256, 0, s>>>(list, lc, hp, codes, req, a_next, xlist, lc + 2, slot, g,
-                                                         div_nx);
-            k_detect_exact<T><<<list_blocks, 256, 0, s>>>(xlist, lc + 2, fh, codes, req, a_next, slot, g, div_nx);
-            launches += 4;
         } else {
             k_sparse_px<T><<<list_grid(g), kListBlock, 0, s>>>(fh, hp, codes, act[cur], a_next, req, slot, g);
             ++launches;
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
-        if (use_list) {
-            uint32_t *lc = lcnt + 3 * sweeps + 1;
-            compact_bitmap(req, g, bcnt, list, lc, s);
-            k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, lc, f, fh, cnt, hp, a_next, slot, g, div_nx, eps, delta, q);
-            launches += 3;
-        } else {
-            k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
-            ++launches;
-        }
+        k_apply_px<T><<<list_grid(g), kListBlock, 0, s>>>(f, fh, cnt, hp, req, a_next, slot, g, eps, delta, q);
+        ++launches;
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[2], s));
         PMSZ_CUDA(cudaGetLastError());
         PMSZ_CUDA(cudaMemcpyAsync(hslot, slot, sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
@@ -447,8 +558,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         // Once the next active set is small, per-sweep launches and host round
         // trips dominate: hand the remaining sweeps to one cooperative launch.
         const unsigned long long est_next = 15ull * h.changed + h.fdir;
-        if (!(flags & PMSZ_FLAG_FULL_SWEEPS) && sweeps < max_sweeps &&
-            est_next <= std::max<unsigned long long>(g.n / 32, 1ull << 16)) {
+        if (!(flags & PMSZ_FLAG_FULL_SWEEPS) && sweeps < max_sweeps && est_next <= tail_at) {
             int64_t done = 0;
             if ((rc = run_sweep_loop<T>(f, fh, codes, cnt, hp, req, act, slots, sweeps, max_sweeps, g, eps, delta, q,
                                         s, timing ? &et : nullptr, &ms_detect, &done)))

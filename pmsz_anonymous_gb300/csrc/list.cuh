@@ -49,8 +49,9 @@ __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t *s_warp) 
 }
 
 __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *__restrict__ bm, Geom g,
-                                                               uint32_t *__restrict__ counts) {
+                                                               uint32_t *__restrict__ counts, const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
+    if (run && *run == 0) return;
     const size_t per = compact_per(g);
     const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(g.nwords, lo + per);
     uint32_t c = 0;
@@ -72,9 +73,11 @@ __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *_
 constexpr uint32_t kStage = 8192;
 __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
                                                               const uint32_t *__restrict__ counts,
-                                                              uint32_t *__restrict__ list, uint32_t *total) {
+                                                              uint32_t *__restrict__ list, uint32_t *total,
+                                                              const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
     __shared__ uint32_t s_stage[kStage];
+    if (run && *run == 0) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t before = 0, all = 0;
     for (int b = t; b < static_cast<int>(gridDim.x); b += kCompactBlock) {
@@ -173,9 +176,10 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
                                                      const uint32_t *__restrict__ hp, const uint8_t *__restrict__ codes,
                                                      uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
                                                      uint32_t *__restrict__ exact_list, uint32_t *exact_count,
-                                                     SweepSlot *slot, Geom g, FastDiv div_nx) {
+                                                     SweepSlot *slot, Geom g, FastDiv div_nx, const int *run) {
     __shared__ uint32_t s_exact[kExactCap];
     __shared__ uint32_t s_n, s_base;
+    if (run && *run == 0) return;
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
     const uint32_t m = *count;
@@ -219,7 +223,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_detect_exact(const uint32_t *__restrict__ exact_list, const uint32_t *count,
                                                       const T *__restrict__ fh, const uint8_t *__restrict__ codes,
                                                       uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
-                                                      SweepSlot *slot, Geom g, FastDiv div_nx) {
+                                                      SweepSlot *slot, Geom g, FastDiv div_nx, const int *run) {
+    if (run && *run == 0) return;
     const uint32_t m = *count;
     uint32_t cmax = 0, cmin = 0, cdir = 0;
     const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
@@ -251,7 +256,8 @@ __global__ void __launch_bounds__(256) k_apply_list(const uint32_t *__restrict__
                                                     const T *__restrict__ f, T *__restrict__ fh,
                                                     uint8_t *__restrict__ cnt, uint32_t *__restrict__ hp,
                                                     uint32_t *__restrict__ act_next, SweepSlot *slot, Geom g,
-                                                    FastDiv div_nx, T eps, T delta, int q) {
+                                                    FastDiv div_nx, T eps, T delta, int q, const int *run) {
+    if (run && *run == 0) return;
     const uint32_t m = *count;
     uint32_t nreq = 0, nchg = 0, nprog = 0;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
@@ -287,11 +293,45 @@ __global__ void __launch_bounds__(256) k_apply_list(const uint32_t *__restrict__
 }
 
 // Bitmap -> list (k_count_words, k_write_list); counts: kCompactBlocks words of
-// scratch; *total receives the list length.
+// scratch; *total receives the list length.  run (or null): the sweep's gate.
 inline void compact_bitmap(uint32_t *bm, const Geom &g, uint32_t *counts, uint32_t *list, uint32_t *total,
-                           cudaStream_t s) {
-    k_count_words<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts);
-    k_write_list<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts, list, total);
+                           const int *run, cudaStream_t s) {
+    k_count_words<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts, run);
+    k_write_list<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts, list, total, run);
+}
+
+// State of the device-side sweep loop: the index of the sweep that runs
+// next, its gate, its list lengths and its counters (copied to the sweep's
+// slot by k_loop_gate).
+struct LoopState {
+    long long k;
+    int go;
+    int pad;
+    uint32_t lc[4];  // active list, request list, exact list
+    SweepSlot cur;
+};
+
+// After sweep ls->k: store its counters, decide whether the next sweep runs
+// (not converged, not stuck, no NaN input at sweep 0, sweeps left, and an
+// active set still too large for the cooperative tail: 15 * changed + fdir >
+// tail_at), advance k, clear the per-sweep state, and, in the loop body, set
+// the condition of the graph's while node.
+__global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long max_sweeps, unsigned long long tail_at,
+                            cudaGraphConditionalHandle cond, int set_cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (ls->go) {
+        const SweepSlot c = ls->cur;
+        const long long k = ls->k;
+        slots[k] = c;
+        const bool stop = (k == 0 && c.bad) || (c.fmax == 0 && c.fmin == 0 && c.fdir == 0) || c.progressed == 0 ||
+                          k + 1 >= max_sweeps;
+        const bool tail = 15ull * c.changed + c.fdir <= tail_at;
+        ls->go = (!stop && !tail) ? 1 : 0;
+        ls->k = k + 1;
+        ls->cur = SweepSlot{};
+        ls->lc[0] = ls->lc[1] = ls->lc[2] = ls->lc[3] = 0;
+    }
+    if (set_cond) cudaGraphSetConditional(cond, ls->go ? 1u : 0u);
 }
 
 }  // namespace pmsz
