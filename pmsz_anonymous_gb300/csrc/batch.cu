@@ -33,7 +33,7 @@ __device__ __forceinline__ int find_seg(const uint32_t *__restrict__ pre, int n,
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 5) k_first_multi(const Inst<T> *__restrict__ inst,
                                                             const uint32_t *__restrict__ tpre, int n) {
-    __shared__ TileSmem<T, 2> sm;
+    __shared__ TileSmem<T, 2, true> sm;
     const int i = find_seg(tpre, n, blockIdx.x);
     const Inst<T> &I = inst[i];
     if (!I.first) return;  // uniform: only fields that start now

@@ -266,7 +266,8 @@ int check_geom(size_t nx, size_t ny, size_t nz) {
 // waits for the next slab's event (its tiles read one plane beyond the slab).
 template <typename T>
 int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
-                      uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches) {
+                      uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches,
+                      uint32_t *xlist, uint32_t *xcount) {
     if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
     const int nchunks = (g.nz + kZChunk - 1) / kZChunk;
@@ -312,7 +313,11 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
         PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
         dim3 grid = tiled_grid(g);
         grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
-        k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
+        if (xlist)  // deferring first pass (see k_first_exact)
+            k_tiled<T, kFirst, true><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps, xlist,
+                                                            xcount);
+        else
+            k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
         PMSZ_CUDA(cudaGetLastError());
         ++*launches;
     }
@@ -404,12 +409,17 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             PMSZ_CUDA(cudaEventRecord(lt.ev[0], s));
         }
         if (ingest) {
-            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches)))
+            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches, xlist,
+                                           &ls->lc[3])))
                 return rc;
         } else {
-            k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act[1], &ls->cur, g, 0);
+            k_tiled<T, kFirst, true><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act[1], &ls->cur, g, 0,
+                                                                     xlist, &ls->lc[3]);
             ++launches;
         }
+        k_first_exact<T><<<list_blocks, 256, 0, s>>>(xlist, &ls->lc[3], f, fh, codes, req, act[1], &ls->cur, g,
+                                                     div_nx);
+        ++launches;
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[1], s));
         compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, s);
         k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, act[1], &ls->cur, g, div_nx, eps,
@@ -516,7 +526,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         uint32_t *a_next = act[cur ^ 1];
         if (timing) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
         if (sweeps == 0 && ingest) {
-            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, a_next, slot, g, s, &launches))) return rc;
+            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, a_next, slot, g, s, &launches, nullptr,
+                                           nullptr)))
+                return rc;
         } else if (sweeps == 0) {
             k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, 0);
             ++launches;

@@ -248,6 +248,45 @@ __global__ void __launch_bounds__(256) k_detect_exact(const uint32_t *__restrict
     block_flush_slot(slot, v);
 }
 
+// Voxels the first pass deferred (a failed certificate in f or fhat): the
+// original code byte and the first detection on the full keys of both fields.
+template <typename T>
+__global__ void __launch_bounds__(256) k_first_exact(const uint32_t *__restrict__ xlist, const uint32_t *count,
+                                                     const T *__restrict__ f, const T *__restrict__ fh,
+                                                     uint8_t *__restrict__ codes, uint32_t *__restrict__ req,
+                                                     uint32_t *__restrict__ act_next, SweepSlot *slot, Geom g,
+                                                     FastDiv div_nx) {
+    const uint32_t m = *count;
+    uint32_t cmax = 0, cmin = 0, cdir = 0;
+    const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
+    using K = typename KeyOf<T>::type;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(xlist + k);
+        int x, y, z;
+        voxel_coords(g, div_nx, i, x, y, z);
+        const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        K kk[15];
+        int oasc, odesc, asc, desc;
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+            kk[r] = ((valid >> r) & 1u) ? okey(__ldg(f + (static_cast<ptrdiff_t>(i) + off))) : K(0);
+        }
+        arg_ext(kk, valid, oasc, odesc);
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+            kk[r] = ((valid >> r) & 1u) ? okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off))) : K(0);
+        }
+        arg_ext(kk, valid, asc, desc);
+        const uint8_t c = static_cast<uint8_t>(oasc | (odesc << 4));
+        codes[i] = c;
+        detect_outcome(g, x, y, z, asc, desc, c, req, act_next, cmax, cmin, cdir);
+    }
+    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, 0u, 0u};
+    block_flush_slot(slot, v);
+}
+
 // The edit of every listed voxel (applyDeltaBuffer_local, pMSz.cu:623-645),
 // the proxy refresh, and for a changed value the closed stencil of the voxel
 // in the next active set.

@@ -82,10 +82,22 @@ constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kRing = 4, kZChun
 constexpr int kCells = kHX * kHY, kThreads = kTX * kTY;
 enum TileMode { kFirst = 0, kDetect = 1, kCodes = 2 };
 
+constexpr uint32_t kFirstXCap = 512;  // deferred voxels buffered per block
+
+// KEYS: full keys beside the proxies for an inline exact path; without them
+// (the deferring first pass) a buffer of voxels whose certificate failed.
+template <typename T, int NF, bool KEYS>
+struct TileSmem;
 template <typename T, int NF>
-struct TileSmem {
+struct TileSmem<T, NF, true> {
     uint32_t p[NF][kRing][kHY][kHX];                  // proxies
     typename KeyOf<T>::type k[NF][kRing][kHY][kHX];   // full keys, for the rare exact path
+};
+template <typename T, int NF>
+struct TileSmem<T, NF, false> {
+    uint32_t p[NF][kRing][kHY][kHX];  // proxies
+    uint32_t x[kFirstXCap];           // voxels whose certificate failed
+    uint32_t xn, xbase;
 };
 
 __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; }
@@ -102,12 +114,19 @@ __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; 
 //   kDetect: fa = fhat; the original codes come from `codes` (full sweep).
 //   kCodes : fa = a field; writes its code byte only (pmsz_codes_*).
 // ---------------------------------------------------------------------------
-template <typename T, int MODE>
-__device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &sm, const T *__restrict__ fa,
+//   DEFER (kFirst only, fields of fewer than 2^32 voxels): a voxel whose
+//            certificate fails in either field is not decided here but
+//            appended to xlist (k_first_exact decides it on full keys), so no
+//            warp runs a one-lane exact path inside the plane loop and no
+//            full keys are staged.
+template <typename T, int MODE, bool DEFER = false>
+__device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1, !DEFER> &sm, const T *__restrict__ fa,
                                            const T *__restrict__ fb, uint8_t *__restrict__ codes,
                                            uint32_t *__restrict__ hp, uint32_t *__restrict__ req,
                                            uint32_t *__restrict__ act_next, SweepSlot *slot, const Geom &g, int bx,
-                                           int by, int bz) {
+                                           int by, int bz, uint32_t *__restrict__ xlist = nullptr,
+                                           uint32_t *xcount = nullptr) {
+    static_assert(!DEFER || MODE == kFirst, "only the first pass defers");
     constexpr int NF = MODE == kFirst ? 2 : 1;
     using K = typename KeyOf<T>::type;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
@@ -155,7 +174,8 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
                     }
                 }
                 (&sm.p[F][s][0][0])[cell_s[j]] = px;
-                (&sm.k[F][s][0][0])[cell_s[j]] = key;
+                if constexpr (!DEFER) (&sm.k[F][s][0][0])[cell_s[j]] = key;
+                (void)key;
             }
         }
     };
@@ -165,14 +185,21 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
 #pragma unroll
         for (int r = 0; r < 15; ++r) t[r] = sm.p[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
         Ext e = interior ? proxy_ext_interior(t) : proxy_ext(t);
-        if (!e.exact) {  // ties in the truncated proxies: exact keys
-            K k[15];
+        if constexpr (!DEFER) {
+            if (!e.exact) {  // ties in the truncated proxies: exact keys
+                K k[15];
 #pragma unroll
-            for (int r = 0; r < 15; ++r) k[r] = sm.k[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
-            arg_ext(k, valid_mask(x, y, z, g.nx, g.ny, g.nz), e.asc, e.desc);
+                for (int r = 0; r < 15; ++r)
+                    k[r] = sm.k[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+                arg_ext(k, valid_mask(x, y, z, g.nx, g.ny, g.nz), e.asc, e.desc);
+                e.exact = true;
+            }
         }
         return e;
     };
+    if constexpr (DEFER) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) sm.xn = 0;  // made visible by the prologue barrier
+    }
 
     load_plane(zb - 1);
     load_plane(zb);
@@ -194,20 +221,32 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
             } else {
                 int oasc, odesc;
                 Ext e;
+                bool decided = true;
                 if (MODE == kFirst) {
                     const Ext o = ext(0, z, slots, interior);
                     oasc = o.asc;
                     odesc = o.desc;
-                    codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
                     e = ext(1, z, slots, interior);
+                    if (DEFER && !(o.exact && e.exact)) {
+                        decided = false;
+                        if constexpr (DEFER) {
+                            const uint32_t pos = atomicAdd(&sm.xn, 1u);
+                            if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
+                            else xlist[atomicAdd(xcount, 1u)] = static_cast<uint32_t>(i);
+                        }
+                    } else {
+                        codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
+                    }
                 } else {
                     const uint8_t c = codes[i];
                     oasc = c & 15;
                     odesc = c >> 4;
                     e = ext(0, z, slots, interior);
                 }
-                tm = detect_rules(e.asc, e.desc, oasc, odesc, cmax, cmin, cdir);
-                if (tm) request_targets(req, g, x, y, z, tm);
+                if (decided) {
+                    tm = detect_rules(e.asc, e.desc, oasc, odesc, cmax, cmin, cdir);
+                    if (tm) request_targets(req, g, x, y, z, tm);
+                }
                 ++active;
             }
         }
@@ -221,18 +260,26 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1> &
         const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, bad};
         block_flush_slot(slot, v);
     }
+    if constexpr (DEFER) {  // sm.xn is final: the plane loop ended with a barrier
+        const uint32_t nb = min(sm.xn, kFirstXCap);
+        const int tid2 = threadIdx.y * kTX + threadIdx.x;
+        if (tid2 == 0) sm.xbase = nb ? atomicAdd(xcount, nb) : 0u;
+        __syncthreads();
+        for (uint32_t j = tid2; j < nb; j += kThreads) xlist[sm.xbase + j] = sm.x[j];
+    }
 }
 
 // bz0: index of the first z-chunk the launch covers (a launch may cover a
 // z-range of chunks, e.g. the part of the field already copied in).
-template <typename T, int MODE>
+template <typename T, int MODE, bool DEFER = false>
 __global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
                                                        uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
                                                        uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
-                                                       SweepSlot *slot, Geom g, int bz0) {
-    __shared__ TileSmem<T, MODE == kFirst ? 2 : 1> sm;
-    tiled_body<T, MODE>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y,
-                        bz0 + static_cast<int>(blockIdx.z));
+                                                       SweepSlot *slot, Geom g, int bz0, uint32_t *xlist = nullptr,
+                                                       uint32_t *xcount = nullptr) {
+    __shared__ TileSmem<T, MODE == kFirst ? 2 : 1, !DEFER> sm;
+    tiled_body<T, MODE, DEFER>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y,
+                               bz0 + static_cast<int>(blockIdx.z), xlist, xcount);
 }
 
 // ---------------------------------------------------------------------------
