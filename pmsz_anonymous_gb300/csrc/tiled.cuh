@@ -272,7 +272,7 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1, !
 // bz0: index of the first z-chunk the launch covers (a launch may cover a
 // z-range of chunks, e.g. the part of the field already copied in).
 template <typename T, int MODE, bool DEFER = false>
-__global__ void __launch_bounds__(kThreads, 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
+__global__ void __launch_bounds__(kThreads, MODE == kFirst && DEFER ? 6 : 5) k_tiled(const T *__restrict__ fa, const T *__restrict__ fb,
                                                        uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
                                                        uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
                                                        SweepSlot *slot, Geom g, int bz0, uint32_t *xlist = nullptr,
