@@ -329,7 +329,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n + n_clamp * itemsize,
                 "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY: H2D f and fhat, correction, "
                         "edit extraction, D2H delta symbols (1 B/voxel) and clamp list"},
-        "roofline": {"bound": "hbm", "kernel": "k_tiled<T,kFirst> (labelling + first detection)",
+        "roofline": {"bound": "hbm", "kernel": "k_tiled<T,kFirst,DEFER> + k_first_exact (labelling + first detection)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": bytes_first,
                      "ms_per_launch": statistics.mean(first_ms),

@@ -203,3 +203,27 @@ def test_medium_field_against_oracle(cuda):
     assert r.status == st == capi.PMSZ_OK
     np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
     np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+@pytest.mark.parametrize("dtype,comp", [(torch.float32, "zfp"), (torch.float64, "sz3")])
+def test_large_field_through_the_device_sweep_loop(cuda, dtype, comp):
+    """256^3: several list sweeps run inside the CUDA-graph loop (the active
+    set after the first pass is far above the tail threshold) before the
+    cooperative tail; field, sweep count and every per-sweep record equal the
+    oracle's, and FULL_SWEEPS (host-driven full sweeps) gives the same."""
+    shape, eb = (256, 256, 256), 1e-4
+    df = api().gen_perlin(shape, 3, 5, 1 / 64, dtype=dtype)
+    dfh = api().standin(df, eb, comp, 3)
+    f, fh = df.cpu().numpy(), dfh.cpu().numpy()
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    work = dfh.clone()
+    r = api().correct(df, work, eb)
+    assert r.status == st == capi.PMSZ_OK
+    assert r.sweeps == sw
+    assert int(r.log[1, 6]) > max(f.size // 32, 1 << 16)  # sweep 2 runs as a list sweep
+    np.testing.assert_array_equal(work.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
+    full = dfh.clone()
+    rf = api().correct(df, full, eb, full_sweeps=True)
+    assert rf.sweeps == sw
+    assert torch.equal(full.view(torch.uint8), work.view(torch.uint8))
