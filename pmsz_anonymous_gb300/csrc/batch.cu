@@ -12,6 +12,7 @@
 // continuous-batching server (server.cpp), where fields join and leave between
 // sweeps.
 #include "batch.h"
+#include "batch_list.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -192,8 +193,27 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
     const size_t o_inst = ws.reserve<Inst<T>>(n);
     const size_t o_pre = ws.reserve<uint32_t>(2 * (n + 1));
     const size_t o_iters = ws.reserve<long long>(1);
+    std::vector<Geom> geoms(n);
+    for (int i = 0; i < n; ++i) geoms[i] = host[i].g;
+    std::vector<uint32_t> wpre;
+    uint64_t total_voxels = 0;
+    for (const Geom &g : geoms) total_voxels += g.n;
+    lists = list_prefixes(geoms, wpre, ml.total_words);
+    const size_t o_wpre = ws.reserve<uint32_t>(lists ? n + 1 : 0);
+    const size_t o_cnts = ws.reserve<uint32_t>(lists ? kCompactBlocks : 0);
+    const size_t o_list = ws.reserve<uint64_t>(lists ? total_voxels : 0);
+    const size_t o_xlist = ws.reserve<uint64_t>(lists ? total_voxels : 0);
+    const size_t o_lc = ws.reserve<uint32_t>(lists ? 4 : 0);
     int rc = ws.commit();
     if (rc) return rc;
+    if (lists) {
+        ml.wpre = ws.at<uint32_t>(o_wpre);
+        ml.counts = ws.at<uint32_t>(o_cnts);
+        ml.list = ws.at<uint64_t>(o_list);
+        ml.xlist = ws.at<uint64_t>(o_xlist);
+        ml.lc = ws.at<uint32_t>(o_lc);
+        PMSZ_CUDA(cudaMemcpyAsync(ml.wpre, wpre.data(), wpre.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    }
     unsigned char *zero = ws.at<unsigned char>(o_zero), *other = ws.at<unsigned char>(o_other);
     slots = reinterpret_cast<SweepSlot *>(zero + zero_bytes);
     for (int i = 0; i < n; ++i) {
@@ -242,8 +262,10 @@ __global__ void k_gather_slots(const Inst<T> *__restrict__ inst, int n, SweepSlo
 
 template <typename T>
 int launch_generation(const Inst<T> *dinst, const uint32_t *dtpre, const uint32_t *drpre, int n,
-                      uint32_t total_tiles, uint32_t total_rounds, bool any_first, cudaStream_t s) {
+                      uint32_t total_tiles, uint32_t total_rounds, bool any_first, cudaStream_t s,
+                      const MultiLists *ml) {
     if (any_first) k_first_multi<T><<<total_tiles, dim3(kTX, kTY, 1), 0, s>>>(dinst, dtpre, n);
+    if (ml) return launch_list_sweep<T>(dinst, n, *ml, s);
     const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(total_rounds, 152 * 16)));
     k_phase_multi<T, 0><<<grid, kListBlock, 0, s>>>(dinst, drpre, n, total_rounds);
     k_phase_multi<T, 1><<<grid, kListBlock, 0, s>>>(dinst, drpre, n, total_rounds);
@@ -259,9 +281,9 @@ int launch_gather(const Inst<T> *dinst, int n, SweepSlot *out, cudaStream_t s) {
 }
 
 template int launch_generation<float>(const Inst<float> *, const uint32_t *, const uint32_t *, int, uint32_t,
-                                      uint32_t, bool, cudaStream_t);
+                                      uint32_t, bool, cudaStream_t, const MultiLists *);
 template int launch_generation<double>(const Inst<double> *, const uint32_t *, const uint32_t *, int, uint32_t,
-                                       uint32_t, bool, cudaStream_t);
+                                       uint32_t, bool, cudaStream_t, const MultiLists *);
 template int launch_gather<float>(const Inst<float> *, int, SweepSlot *, cudaStream_t);
 template int launch_gather<double>(const Inst<double> *, int, SweepSlot *, cudaStream_t);
 
@@ -271,7 +293,9 @@ int MultiRun<T>::generation() {
     if (rc) return rc;
     bool any_first = false;
     for (const Inst<T> &I : host) any_first |= I.first != 0;
-    if ((rc = launch_generation<T>(dinst, dtpre, drpre, n, total_tiles, total_rounds, any_first, s))) return rc;
+    if ((rc = launch_generation<T>(dinst, dtpre, drpre, n, total_tiles, total_rounds, any_first, s,
+                                   lists ? &ml : nullptr)))
+        return rc;
     for (Inst<T> &I : host) I.first = 0;
     return PMSZ_OK;
 }

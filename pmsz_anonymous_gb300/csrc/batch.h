@@ -45,6 +45,15 @@ struct BatchOutcome {
     std::vector<SweepSlot> log;
 };
 
+// Scratch of the voxel-list generations of a table of fields (batch_list.cuh).
+struct MultiLists {
+    uint32_t *wpre = nullptr;   // n + 1 word prefixes (multiples of 4), device
+    uint64_t total_words = 0;
+    uint32_t *counts = nullptr; // one count per compaction block (kCompactBlocks)
+    uint64_t *list = nullptr, *xlist = nullptr;  // capacity: the fields' voxels
+    uint32_t *lc = nullptr;     // 4 list lengths
+};
+
 // Scratch and table of one multi-field run; slot rows are sweep-major
 // (row k holds the slot of sweep k of every field).
 template <typename T>
@@ -72,13 +81,34 @@ struct MultiRun {
     uint32_t *dtpre = nullptr, *drpre = nullptr;
     long long *diters = nullptr;
     SweepSlot *slots = nullptr;
+    MultiLists ml;
+    bool lists = false;  // voxel-list generations (all fields together below 2^32 voxels)
 };
 
 // One generation over a device table of n fields (see MultiRun::generation),
 // and the gather of each field's current-sweep slot into out[0..n).
+// ml: the voxel-list scratch, or null for the round-based passes.
 template <typename T>
 int launch_generation(const Inst<T> *dinst, const uint32_t *dtpre, const uint32_t *drpre, int n,
-                      uint32_t total_tiles, uint32_t total_rounds, bool any_first, cudaStream_t s);
+                      uint32_t total_tiles, uint32_t total_rounds, bool any_first, cudaStream_t s,
+                      const MultiLists *ml);
+
+// Word prefixes of a table (each field's bitmap words rounded up to a multiple
+// of 4) and their total; false if the list form does not apply (the fields'
+// voxels or words reach 2^32).
+inline bool list_prefixes(const std::vector<Geom> &geoms, std::vector<uint32_t> &wpre, uint64_t &total_words) {
+    wpre.assign(geoms.size() + 1, 0);
+    uint64_t words = 0, voxels = 0;
+    for (size_t i = 0; i < geoms.size(); ++i) {
+        wpre[i] = static_cast<uint32_t>(words);
+        words += (geoms[i].nwords + 3) & ~static_cast<size_t>(3);
+        voxels += geoms[i].n;
+        if (words >= (1ull << 32) || voxels >= (1ull << 32)) return false;
+    }
+    wpre[geoms.size()] = static_cast<uint32_t>(words);
+    total_words = words;
+    return true;
+}
 template <typename T>
 int launch_gather(const Inst<T> *dinst, int n, SweepSlot *out, cudaStream_t s);
 

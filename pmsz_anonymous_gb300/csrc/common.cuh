@@ -153,6 +153,9 @@ __host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) 
     return static_cast<uint32_t>((static_cast<uint64_t>(t) + n) >> f.s);
 }
 
+// Blocks of the bitmap-compaction kernels (one contiguous word range each).
+constexpr int kCompactBlocks = 152 * 8;
+
 // Field geometry.  Bitmaps hold one bit per voxel with every x-row padded to
 // whole 32-bit words: word (wx, y, z) = wx + wpr*(y + ny*z), bit b = x - 32*wx.
 struct Geom {
@@ -160,7 +163,7 @@ struct Geom {
     int wpr;          // words per x-row
     size_t nwords;    // wpr * ny * nz (< 2^32)
     size_t n;         // nx * ny * nz
-    FastDiv div_wpr, div_ny;
+    FastDiv div_wpr, div_ny, div_nx;  // div_nx: for flat indices below 2^32
 };
 
 inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
@@ -173,6 +176,7 @@ inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
     g.n = nx * ny * nz;
     g.div_wpr = make_fastdiv(static_cast<uint32_t>(g.wpr));
     g.div_ny = make_fastdiv(static_cast<uint32_t>(ny));
+    g.div_nx = make_fastdiv(static_cast<uint32_t>(nx));
     return g;
 }
 

@@ -31,7 +31,6 @@ constexpr int kCompactWords = kCompactBlock * 4;  // one uint4 of words per thre
 // words; k_write_list derives its block's offset from the counts before it,
 // writes the flat indices of its range in order and clears the words.  Block b
 // of both kernels covers words [b * per, (b + 1) * per), per a multiple of 4.
-constexpr int kCompactBlocks = 152 * 8;
 
 __host__ __device__ __forceinline__ size_t compact_per(const Geom &g) {
     return ((g.nwords + kCompactBlocks - 1) / kCompactBlocks + 3) & ~static_cast<size_t>(3);
@@ -48,7 +47,7 @@ __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t *s_warp) 
     return tot;
 }
 
-__global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *__restrict__ bm, Geom g,
+static __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *__restrict__ bm, Geom g,
                                                                uint32_t *__restrict__ counts, const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
     if (run && *run == 0) return;
@@ -67,16 +66,69 @@ __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *_
     if (threadIdx.x == 0) counts[blockIdx.x] = c;
 }
 
-// Four words per thread per step (one 16-byte load); the step's first
-// kStage entries are staged in shared memory in order and copied out with
-// coalesced stores, any beyond (only in very dense steps) go out directly.
-constexpr uint32_t kStage = 8192;
-__global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
+// Writes the entries of one compaction step (the block's kCompactWords
+// bitmap words, four per thread in w) to out[0 .. step) in word order; base(j)
+// gives the entry of bit 0 of the thread's word j (a word's entries are base
+// + bit), lane_ex is the thread's exclusive prefix of bit counts within its
+// warp and wbase its warp's offset in the step.  Block-uniform choice:
+//  - the step fits the 32 KB staging buffer: every thread writes its own
+//    entries into shared memory at their ranks, then the block copies the
+//    step out with coalesced stores;
+//  - denser steps: the words and their bases are staged per warp and the
+//    warp visits its non-zero words in order, every lane writing the entry of
+//    its own bit of the word at the bit's rank, so each word's entries go out
+//    as one contiguous store and no thread loops over more than its bit.
+constexpr uint32_t kStageBytes = 32768;
+template <typename E, class Base>
+__device__ __forceinline__ void write_step_entries(const uint32_t (&w)[4], uint32_t lane_ex, uint32_t wbase,
+                                                   uint32_t step, unsigned char *raw, E *out, Base &&base) {
+    constexpr uint32_t kCap = kStageBytes / sizeof(E);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (step <= kCap) {
+        E *st = reinterpret_cast<E *>(raw);
+        uint32_t p = wbase + lane_ex;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (!w[j]) continue;
+            const E b0 = base(j);
+            for (uint32_t bits = w[j]; bits; bits &= bits - 1) st[p++] = b0 + static_cast<E>(__ffs(bits) - 1);
+        }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < step; e += blockDim.x) out[e] = st[e];
+        __syncthreads();  // the buffer is reused by the next step
+        return;
+    }
+    uint32_t *sw = reinterpret_cast<uint32_t *>(raw) + warp * 128;
+    E *sb = reinterpret_cast<E *>(raw + 4 * kCompactWords) + warp * 128;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        sw[lane * 4 + j] = w[j];
+        sb[lane * 4 + j] = w[j] ? base(j) : E(0);
+    }
+    __syncwarp();
+    const uint32_t below = (1u << lane) - 1u;
+    E *wo = out + wbase;
+    uint32_t run = 0;
+#pragma unroll
+    for (int gi = 0; gi < 4; ++gi) {
+        for (uint32_t nz = __ballot_sync(0xFFFFFFFFu, sw[gi * 32 + lane] != 0u); nz; nz &= nz - 1) {
+            const int k = gi * 32 + __ffs(nz) - 1;
+            const uint32_t word = sw[k];
+            if ((word >> lane) & 1u) wo[run + __popc(word & below)] = sb[k] + static_cast<E>(lane);
+            run += __popc(word);
+        }
+    }
+    __syncthreads();  // the buffer is reused by the next step
+}
+
+// Four words per thread per step (one 16-byte load), written with
+// write_step_entries.
+static __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
                                                               const uint32_t *__restrict__ counts,
                                                               uint32_t *__restrict__ list, uint32_t *total,
                                                               const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
-    __shared__ uint32_t s_stage[kStage];
+    __shared__ __align__(16) unsigned char s_raw[kStageBytes];
     if (run && *run == 0) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t before = 0, all = 0;
@@ -110,39 +162,43 @@ __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restri
         uint32_t inc = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-            if (lane >= o) inc += v;
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += u;
         }
         if (lane == 31) s_warp[warp] = inc;
         __syncthreads();
         uint32_t wbase = 0, step = 0;
         for (int k = 0; k < kCompactBlock / 32; ++k) {
-            const uint32_t v = s_warp[k];
-            if (k < warp) wbase += v;
-            step += v;
+            const uint32_t u = s_warp[k];
+            if (k < warp) wbase += u;
+            step += u;
         }
-        if (c) {
-            uint32_t p = wbase + inc - c;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (!w[j]) continue;
-                const uint32_t wj = static_cast<uint32_t>(w0 + j);
-                const uint32_t row = fdiv(wj, g.div_wpr);
-                const uint32_t wx = wj - row * static_cast<uint32_t>(g.wpr);
-                const uint32_t i0 = row * static_cast<uint32_t>(g.nx) + (wx << 5);
-                for (uint32_t bits = w[j]; bits; bits &= bits - 1, ++p) {
-                    const uint32_t e = i0 + static_cast<uint32_t>(__ffs(bits) - 1);
-                    if (p < kStage) s_stage[p] = e;
-                    else list[pos + p] = e;
-                }
-            }
-        }
-        __syncthreads();
-        const uint32_t staged = min(step, kStage);
-        for (uint32_t e = t; e < staged; e += kCompactBlock) list[pos + e] = s_stage[e];
-        pos += step;
-        __syncthreads();  // s_warp / s_stage are rewritten by the next step
+        const uint32_t mine = static_cast<uint32_t>(w0);  // nwords < 2^27 in the list form
+        write_step_entries(w, inc - c, wbase, step, s_raw, list + pos, [&](int j) {
+            const uint32_t wj = mine + static_cast<uint32_t>(j);
+            const uint32_t row = fdiv(wj, g.div_wpr);
+            const uint32_t wx = wj - row * static_cast<uint32_t>(g.wpr);
+            return row * static_cast<uint32_t>(g.nx) + (wx << 5);
+        });
+        pos += step;  // write_step_entries ends with a barrier: s_warp is free
     }
+}
+
+// Lanes whose voxels share a bitmap word carry the same key; in a list in
+// voxel order they are consecutive lanes.  ORs the changed bits cb over each
+// group (a suffix OR within the group) and returns true on the group's lowest
+// lane when the merged bits are non-zero: that lane marks the word's closed
+// stencil once for the whole group.
+template <typename K>
+__device__ __forceinline__ bool warp_merge_word(K key, uint32_t &cb) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_down_sync(0xFFFFFFFFu, cb, o);
+        if (lane + o < 32 && ((grp >> (lane + o)) & 1u)) cb |= u;
+    }
+    return cb && lane == static_cast<uint32_t>(__ffs(grp) - 1);
 }
 
 // Coordinates of a flat index (n < 2^32).
@@ -299,33 +355,40 @@ __global__ void __launch_bounds__(256) k_apply_list(const uint32_t *__restrict__
     if (run && *run == 0) return;
     const uint32_t m = *count;
     uint32_t nreq = 0, nchg = 0, nprog = 0;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
-        const uint32_t v = __ldg(list + k);
-        const T old = fh[v];
-        const uint8_t oc = cnt[v];
-        const T fv = __ldg(f + v);
-        const T lowered = old - delta;
-        T nv;
-        uint8_t nc;
-        if (fabs(fv - lowered) <= eps && static_cast<int>(oc) < q - 1) {
-            nv = lowered;
-            nc = static_cast<uint8_t>(oc + 1);
-        } else {
-            nc = static_cast<uint8_t>(q);
-            nv = fv - eps;
-        }
-        fh[v] = nv;
-        cnt[v] = nc;
-        const bool chg = bits_of(old) != bits_of(nv);
-        ++nreq;
-        nprog += (chg || nc != oc) ? 1u : 0u;
-        if (chg) {
-            ++nchg;
-            hp[v] = proxy_of(nv);
-            int x, y, z;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < m; k0 += gridDim.x * blockDim.x) {
+        const uint32_t k = k0 + lane;  // k0 is warp-uniform
+        uint32_t key = 0xFFFFFFFFu, cb = 0;
+        int x = 0, y = 0, z = 0;
+        if (k < m) {
+            const uint32_t v = __ldg(list + k);
+            const T old = fh[v];
+            const uint8_t oc = cnt[v];
+            const T fv = __ldg(f + v);
+            const T lowered = old - delta;
+            T nv;
+            uint8_t nc;
+            if (fabs(fv - lowered) <= eps && static_cast<int>(oc) < q - 1) {
+                nv = lowered;
+                nc = static_cast<uint8_t>(oc + 1);
+            } else {
+                nc = static_cast<uint8_t>(q);
+                nv = fv - eps;
+            }
+            fh[v] = nv;
+            cnt[v] = nc;
+            const bool chg = bits_of(old) != bits_of(nv);
+            ++nreq;
+            nprog += (chg || nc != oc) ? 1u : 0u;
             voxel_coords(g, div_nx, v, x, y, z);
-            mark_stencil(act_next, g, x >> 5, y, z, 1u << (x & 31));
+            key = v - static_cast<uint32_t>(x & 31);
+            if (chg) {
+                ++nchg;
+                hp[v] = proxy_of(nv);
+                cb = 1u << (x & 31);
+            }
         }
+        if (warp_merge_word(key, cb)) mark_stencil(act_next, g, x >> 5, y, z, cb);
     }
     const uint32_t v[8] = {0u, 0u, 0u, nreq, nchg, nprog, 0u, 0u};
     block_flush_slot(slot, v);
@@ -355,7 +418,7 @@ struct LoopState {
 // active set still too large for the cooperative tail: 15 * changed + fdir >
 // tail_at), advance k, clear the per-sweep state, and, in the loop body, set
 // the condition of the graph's while node.
-__global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long max_sweeps, unsigned long long tail_at,
+static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long max_sweeps, unsigned long long tail_at,
                             cudaGraphConditionalHandle cond, int set_cond) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (ls->go) {

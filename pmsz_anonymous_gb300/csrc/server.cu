@@ -121,7 +121,8 @@ public:
         j->fd = fd;
         j->g = make_geom(fd.nx, fd.ny, fd.nz);
         j->scratch_bytes = field_scratch_bytes(j->g, cfg_.max_sweeps);
-        j->bytes = j->scratch_bytes + 2 * j->g.n * fd.elem_size;
+        // its fields, its scratch, and its share of the group's voxel lists
+        j->bytes = j->scratch_bytes + 2 * j->g.n * fd.elem_size + 2 * sizeof(uint64_t) * j->g.n;
         if (cfg_.hbm_budget_bytes && j->bytes > cfg_.hbm_budget_bytes)
             return set_error(PMSZ_ERR_OOM, "job larger than the server's HBM budget");
         j->t_submit = Clock::now();
@@ -174,6 +175,9 @@ private:
         uint32_t *dpre = nullptr;
         SweepSlot *dslots = nullptr, *hslots = nullptr;
         int cap = 0;
+        MultiLists ml;            // voxel-list scratch of the running set
+        uint32_t *dwpre = nullptr;
+        size_t list_cap = 0;      // entries of ml.list / ml.xlist
     };
 
     template <typename T>
@@ -188,6 +192,27 @@ private:
         PMSZ_CUDA(cudaMalloc(&G.dpre, sizeof(uint32_t) * 2 * (G.cap + 1)));
         PMSZ_CUDA(cudaMalloc(&G.dslots, sizeof(SweepSlot) * G.cap));
         PMSZ_CUDA(cudaMallocHost(&G.hslots, sizeof(SweepSlot) * G.cap));
+        if (G.dwpre) cudaFree(G.dwpre);
+        PMSZ_CUDA(cudaMalloc(&G.dwpre, sizeof(uint32_t) * (G.cap + 1)));
+        return PMSZ_OK;
+    }
+
+    // List buffers for `voxels` entries (grown, never shrunk while the server runs).
+    template <typename T>
+    int ensure_lists(Group<T> &G, size_t voxels) {
+        if (!G.ml.counts) {
+            PMSZ_CUDA(cudaMalloc(&G.ml.counts, sizeof(uint32_t) * kCompactBlocks));
+            PMSZ_CUDA(cudaMalloc(&G.ml.lc, sizeof(uint32_t) * 4));
+        }
+        if (voxels <= G.list_cap) return PMSZ_OK;
+        if (G.ml.list) cudaFree(G.ml.list);
+        if (G.ml.xlist) cudaFree(G.ml.xlist);
+        G.ml.list = G.ml.xlist = nullptr;
+        G.list_cap = 0;
+        const size_t cap = std::max<size_t>(voxels, 1 << 20);
+        PMSZ_CUDA(cudaMalloc(&G.ml.list, sizeof(uint64_t) * cap));
+        PMSZ_CUDA(cudaMalloc(&G.ml.xlist, sizeof(uint64_t) * cap));
+        G.list_cap = cap;
         return PMSZ_OK;
     }
 
@@ -197,6 +222,11 @@ private:
         if (G.dpre) cudaFree(G.dpre);
         if (G.dslots) cudaFree(G.dslots);
         if (G.hslots) cudaFreeHost(G.hslots);
+        if (G.dwpre) cudaFree(G.dwpre);
+        if (G.ml.counts) cudaFree(G.ml.counts);
+        if (G.ml.lc) cudaFree(G.ml.lc);
+        if (G.ml.list) cudaFree(G.ml.list);
+        if (G.ml.xlist) cudaFree(G.ml.xlist);
         G = Group<T>{};
     }
 
@@ -223,10 +253,23 @@ private:
         if (tiles >= (1ull << 31) || rounds >= (1ull << 31)) return set_error(PMSZ_ERR_ARG, "running set too large");
         pre[n] = static_cast<uint32_t>(tiles);
         pre[2 * n + 1] = static_cast<uint32_t>(rounds);
+        std::vector<Geom> geoms(n);
+        size_t voxels = 0;
+        for (int i = 0; i < n; ++i) {
+            geoms[i] = G.host[i].g;
+            voxels += geoms[i].n;
+        }
+        std::vector<uint32_t> wpre;
+        const bool lists = list_prefixes(geoms, wpre, G.ml.total_words);
+        if (lists) {
+            if ((rc = ensure_lists(G, voxels))) return rc;
+            G.ml.wpre = G.dwpre;
+            PMSZ_CUDA(cudaMemcpyAsync(G.dwpre, wpre.data(), sizeof(uint32_t) * wpre.size(), cudaMemcpyHostToDevice, s_));
+        }
         PMSZ_CUDA(cudaMemcpyAsync(G.dinst, G.host.data(), sizeof(Inst<T>) * n, cudaMemcpyHostToDevice, s_));
         PMSZ_CUDA(cudaMemcpyAsync(G.dpre, pre.data(), sizeof(uint32_t) * pre.size(), cudaMemcpyHostToDevice, s_));
         if ((rc = launch_generation<T>(G.dinst, G.dpre, G.dpre + n + 1, n, static_cast<uint32_t>(tiles),
-                                       static_cast<uint32_t>(rounds), any_first, s_)))
+                                       static_cast<uint32_t>(rounds), any_first, s_, lists ? &G.ml : nullptr)))
             return rc;
         if ((rc = launch_gather<T>(G.dinst, n, G.dslots, s_))) return rc;
         PMSZ_CUDA(cudaMemcpyAsync(G.hslots, G.dslots, sizeof(SweepSlot) * n, cudaMemcpyDeviceToHost, s_));

@@ -64,7 +64,7 @@ __device__ __forceinline__ void request_targets_s(uint32_t *req, uint32_t *sum, 
 
 // Summary of a plain bitmap (at the hand-over to the tail): one warp per
 // summary word, lane j testing word j of its 32.
-__global__ void __launch_bounds__(256) k_build_summary(const uint32_t *__restrict__ bm, Geom g,
+static __global__ void __launch_bounds__(256) k_build_summary(const uint32_t *__restrict__ bm, Geom g,
                                                        uint32_t *__restrict__ sum) {
     const size_t ns = summary_words(g);
     const int lane = threadIdx.x & 31;
