@@ -31,6 +31,7 @@ collective; a barrier brackets the timed region and the max over ranks is taken.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import os
 import statistics
@@ -52,6 +53,7 @@ def parse(argv=None):
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--no-tune", action="store_true", help="skip the autotuner (default launch parameters)")
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--shape", default="512,512,512", help="nx,ny,nz")
     p.add_argument("--dtype", choices=["f32", "f64"], default="f64")
@@ -264,6 +266,9 @@ def run_ours(args):
 
     first_ms, times, sweeps, launches, last = [], [], [], 0, None
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # tile depth and pointer-jumping rounds per launch for this shape class,
+    # measured on the inputs themselves (untimed; the timed calls read the table)
+    tune = api.autotune(f, fh0) if not args.no_tune else None
     for _ in range(args.warmup):
         fh.copy_(fh0)
         api.correct(f, fh, args.eb)
@@ -322,6 +327,7 @@ def run_ours(args):
                                                    "from a device copy before each step (untimed)",
                                          "wall_s_timed_region": wall,
                                          "ms_first_pass": statistics.mean(first_ms),
+                                         "autotune": tune,
                                          "ms_detect_sparse": last.ms_detect, "ms_apply": last.ms_apply,
                                          "active_per_sweep": [int(v) for v in last.log[:, 6]],
                                          "requested_per_sweep": [int(v) for v in last.log[:, 3]]}),
@@ -389,6 +395,17 @@ def run_batch(args):
         for w, (_, fh, _) in zip(work, fields):
             w.copy_(fh)
 
+    # tune every shape class of the batch on its first field (untimed); both
+    # forms below then read the same table
+    tune_summary = None
+    if not args.no_tune:
+        api.correct_batch([(f, fh.clone(), eb) for f, fh, eb in fields], autotune=True)
+        chosen = [api.tune_get(f.shape, f.dtype)[1] for f, _, _ in fields]
+        classes = {tuple((int(v) - 1).bit_length() for v in f.shape) for f, _, _ in fields}
+        tune_summary = {"shape_classes": len(classes),
+                        "fields_per_zchunk": dict(collections.Counter(c["zchunk"] for c in chosen)),
+                        "fields_per_jump_rounds": dict(collections.Counter(c["jump_rounds"] for c in chosen))}
+
     def one_by_one():
         for w, (f, _, eb) in zip(work, fields):
             api.correct(f, w, eb)
@@ -426,6 +443,7 @@ def run_batch(args):
         "batch_over_plain": times["plain"] / times["batch"],
         "statuses": sorted(set(r.status for r in res)),
         "sweeps_max": max(r.sweeps for r in res),
+        "autotune": tune_summary,
     }
     print(json.dumps(out), flush=True)
 

@@ -45,6 +45,12 @@ extern "C" {
 #define PMSZ_FLAG_NAIVE 8u        /* pmsz_correct_host_*: run the naive-MSz
                                      strategy (pmsz_correct_naive_*) instead of
                                      the pMSz loop */
+#define PMSZ_FLAG_AUTOTUNE 16u    /* pmsz_correct_{f32,f64} and
+                                     pmsz_correct_batch: a field whose shape
+                                     class has no entry in the tuning table is
+                                     first tuned on its own inputs
+                                     (pmsz_autotune_*); without the flag the
+                                     table is only read */
 
 typedef struct pmsz_opts {
     int32_t q;           /* edit levels; the reference hard-codes q = 5 (pMSz.cu:2630) */
@@ -308,6 +314,44 @@ int pmsz_standin_f32(const float *f, float *fhat, size_t n, double eb, int kind,
                      uint64_t seed, void *stream);
 int pmsz_standin_f64(const double *f, double *fhat, size_t n, double eb, int kind,
                      uint64_t seed, void *stream);
+
+/*
+ * Autotuning.  Two launch parameters are picked per shape class (the ceil-log2
+ * of each axis, and the element size for the tile depth) and kept in a
+ * process-wide table that every entry point reads:
+ *   zchunk      planes per tile column of the fused first pass and the other
+ *               tiled passes (tile 32 x 8 x zchunk); candidates 8, 16, 32, 64;
+ *               default 32.
+ *   jump_rounds pointer-jumping rounds per launch of the label passes
+ *               (pmsz_labels, pmsz_verify_*, the naive strategy): each launch
+ *               lets every voxel take that many three-hop jumps before the
+ *               host reads the convergence flag; candidates 1, 2, 4, 8;
+ *               default 1.
+ * pmsz_autotune_{f32,f64} times every candidate on the given device field pair
+ * (the first pass on f / fhat, then the AS labels of f's codes) on `stream`,
+ * records the fastest in the table and returns the measurements.  Results of
+ * the correction do not depend on either parameter.
+ */
+typedef struct pmsz_tune {
+    int32_t zchunk;
+    int32_t jump_rounds;
+    float ms_zchunk[4];  /* first-pass time per candidate 8, 16, 32, 64 (0: not run) */
+    float ms_rounds[4];  /* AS-label time per candidate 1, 2, 4, 8 (0: not run) */
+} pmsz_tune;
+
+int pmsz_autotune_f32(const float *f, const float *fhat, size_t nx, size_t ny, size_t nz, pmsz_tune *out,
+                      void *stream);
+int pmsz_autotune_f64(const double *f, const double *fhat, size_t nx, size_t ny, size_t nz, pmsz_tune *out,
+                      void *stream);
+/* Table entry of a shape class: returns 1 and fills *out if one is recorded,
+ * else 0 and the defaults (negative: bad arguments). */
+int pmsz_tune_get(size_t nx, size_t ny, size_t nz, size_t elem_size, pmsz_tune *out);
+/* Records an entry (zchunk in 1..256, jump_rounds in 1..16). */
+int pmsz_tune_set(size_t nx, size_t ny, size_t nz, size_t elem_size, const pmsz_tune *t);
+/* Text persistence: one line per entry; load merges into the table. */
+int pmsz_tune_save(const char *path);
+int pmsz_tune_load(const char *path);
+void pmsz_tune_clear(void);
 
 /* Human-readable status, and the last error message of the calling thread. */
 const char *pmsz_strerror(int status);

@@ -25,7 +25,8 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libpmsz_gb300.so")
 CLI = os.path.join(LIBDIR, "pmsz")
 
-CUDA_SOURCES = ["support.cu", "correct.cu", "verify.cu", "edits.cu", "gen.cu", "host.cu", "batch.cu", "server.cu", "naive.cu"]
+CUDA_SOURCES = ["support.cu", "correct.cu", "verify.cu", "edits.cu", "gen.cu", "host.cu", "batch.cu", "server.cu", "naive.cu",
+                "tune.cu"]
 CXX_SOURCES = ["encode.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

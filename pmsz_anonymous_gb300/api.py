@@ -62,10 +62,13 @@ class CorrectResult:
 
 
 def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
-            full_sweeps: bool = False, timing: bool = False, stream=None, strategy: str = "pmsz") -> CorrectResult:
+            full_sweeps: bool = False, timing: bool = False, stream=None, strategy: str = "pmsz",
+            autotune: bool = False) -> CorrectResult:
     """Correct fhat in place so that its extrema and both segmentations match f
     (c_loops, pMSz.cu:1872-2074).  strategy="naive" runs the naive-MSz loop
     instead (naive_MSz.cu:1887-2220; full_sweeps and timing do not apply).
+    autotune=True tunes the field's shape class on these inputs first when the
+    tuning table has no entry for it (PMSZ_FLAG_AUTOTUNE).
     Raises PmszError except for PMSZ_ERR_NOT_CONVERGED, which is reported in
     the result."""
     _check_field(f, "f")
@@ -73,7 +76,8 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
     if f.shape != fhat.shape or f.dtype != fhat.dtype or f.device != fhat.device:
         raise ValueError("f and fhat must share shape, dtype and device")
     L = capi.load()
-    flags = (capi.PMSZ_FLAG_FULL_SWEEPS if full_sweeps else 0) | (capi.PMSZ_FLAG_TIMING if timing else 0)
+    flags = ((capi.PMSZ_FLAG_FULL_SWEEPS if full_sweeps else 0) | (capi.PMSZ_FLAG_TIMING if timing else 0) |
+             (capi.PMSZ_FLAG_AUTOTUNE if autotune else 0))
     opts = capi.Opts(int(q), flags, int(max_sweeps))
     log = (capi.SweepRecord * int(max_sweeps))()
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
@@ -277,9 +281,11 @@ def zstd_version() -> int:
     return int(capi.load().pmsz_zstd_version())
 
 
-def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None):
+def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None, autotune: bool = False):
     """Correct many fields together (pmsz_correct_batch).  items: sequence of
     (f, fhat, eb) CUDA tensors / floats; each fhat is corrected in place.
+    autotune=True tunes every shape class of the batch that the tuning table
+    lacks on its first field first (PMSZ_FLAG_AUTOTUNE).
     Returns a list of CorrectResult, one per item."""
     items = list(items)
     n = len(items)
@@ -298,7 +304,7 @@ def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None):
         fields[k] = capi.Field(f.data_ptr(), fh.data_ptr(), nx, ny, nz, float(eb), f.element_size(), 0)
         results[k].sweep_log = ctypes.cast(logs[k], ctypes.POINTER(capi.SweepRecord))
         results[k].sweep_log_cap = int(max_sweeps)
-    opts = capi.Opts(int(q), 0, int(max_sweeps))
+    opts = capi.Opts(int(q), capi.PMSZ_FLAG_AUTOTUNE if autotune else 0, int(max_sweeps))
     with torch.cuda.device(device):
         st = capi.load().pmsz_correct_batch(fields, n, ctypes.byref(opts), results, statuses, _stream(stream))
     if st not in (capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED, capi.PMSZ_ERR_ARG):
@@ -362,3 +368,56 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def _tune_dict(t) -> dict:
+    return {"zchunk": int(t.zchunk), "jump_rounds": int(t.jump_rounds),
+            "ms_zchunk": {z: float(m) for z, m in zip((8, 16, 32, 64), t.ms_zchunk) if m > 0},
+            "ms_rounds": {r: float(m) for r, m in zip((1, 2, 4, 8), t.ms_rounds) if m > 0}}
+
+
+def autotune(f: torch.Tensor, fhat: torch.Tensor, stream=None) -> dict:
+    """Time the tile depths and pointer-jumping rounds per launch on this field
+    pair (pmsz_autotune_*), record the fastest for its shape class and return
+    the choice with the measured times (ms per candidate)."""
+    _check_field(f, "f")
+    _check_field(fhat, "fhat")
+    if f.shape != fhat.shape or f.dtype != fhat.dtype or f.device != fhat.device:
+        raise ValueError("f and fhat must share shape, dtype and device")
+    t = capi.Tune()
+    nx, ny, nz = _dims(f)
+    with torch.cuda.device(f.device):
+        st = getattr(capi.load(), "pmsz_autotune_" + _suffix(f))(f.data_ptr(), fhat.data_ptr(), nx, ny, nz,
+                                                                 ctypes.byref(t), _stream(stream))
+    capi.check(st)
+    return _tune_dict(t)
+
+
+def tune_get(shape, dtype) -> tuple:
+    """(recorded, {"zchunk", "jump_rounds"}) for a shape (nz, ny, nx) and dtype."""
+    nz, ny, nx = (int(v) for v in shape)
+    t = capi.Tune()
+    st = capi.load().pmsz_tune_get(nx, ny, nz, torch.empty(0, dtype=dtype).element_size(), ctypes.byref(t))
+    if st < 0:
+        capi.check(-st)
+    d = _tune_dict(t)
+    return bool(st), {"zchunk": d["zchunk"], "jump_rounds": d["jump_rounds"]}
+
+
+def tune_set(shape, dtype, zchunk: int, jump_rounds: int) -> None:
+    """Record a tile depth and rounds per launch for the shape class of shape (nz, ny, nx)."""
+    nz, ny, nx = (int(v) for v in shape)
+    t = capi.Tune(int(zchunk), int(jump_rounds))
+    capi.check(capi.load().pmsz_tune_set(nx, ny, nz, torch.empty(0, dtype=dtype).element_size(), ctypes.byref(t)))
+
+
+def tune_save(path: str) -> None:
+    capi.check(capi.load().pmsz_tune_save(str(path).encode()))
+
+
+def tune_load(path: str) -> None:
+    capi.check(capi.load().pmsz_tune_load(str(path).encode()))
+
+
+def tune_clear() -> None:
+    capi.load().pmsz_tune_clear()

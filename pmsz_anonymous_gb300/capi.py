@@ -20,6 +20,7 @@ PMSZ_FLAG_FULL_SWEEPS = 1
 PMSZ_FLAG_TIMING = 2
 PMSZ_FLAG_EDITS_ONLY = 4
 PMSZ_FLAG_NAIVE = 8
+PMSZ_FLAG_AUTOTUNE = 16
 
 
 class Opts(ctypes.Structure):
@@ -55,6 +56,11 @@ class ServerConfig(ctypes.Structure):
 class JobInfo(ctypes.Structure):
     _fields_ = [("done", c_i32), ("status", c_i32), ("sweeps", c_i64), ("edits", c_u64), ("queue_ms", c_double),
                 ("run_ms", c_double), ("latency_ms", c_double)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("zchunk", c_i32), ("jump_rounds", c_i32), ("ms_zchunk", ctypes.c_float * 4),
+                ("ms_rounds", ctypes.c_float * 4)]
 
 
 class HostOutputs(ctypes.Structure):
@@ -99,6 +105,13 @@ SIGNATURES = {
     "pmsz_correct_noalloc": (c_int, [_P, _P, c_size, c_size, c_size, c_size, c_double, _P, _P, _P]),
     "pmsz_correct_host_f32": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
     "pmsz_correct_host_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P, _P, _P]),
+    "pmsz_autotune_f32": (c_int, [_P, _P, c_size, c_size, c_size, _P, _P]),
+    "pmsz_autotune_f64": (c_int, [_P, _P, c_size, c_size, c_size, _P, _P]),
+    "pmsz_tune_get": (c_int, [c_size, c_size, c_size, c_size, _P]),
+    "pmsz_tune_set": (c_int, [c_size, c_size, c_size, c_size, _P]),
+    "pmsz_tune_save": (c_int, [ctypes.c_char_p]),
+    "pmsz_tune_load": (c_int, [ctypes.c_char_p]),
+    "pmsz_tune_clear": (None, []),
 }
 
 _lock = threading.Lock()

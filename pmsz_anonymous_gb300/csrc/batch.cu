@@ -155,7 +155,8 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
     rpre.assign(n + 1, 0);
     uint64_t tiles = 0, rounds = 0;
     for (int i = 0; i < n; ++i) {
-        const Geom g = make_geom(specs[i].nx, specs[i].ny, specs[i].nz);
+        Geom g = make_geom(specs[i].nx, specs[i].ny, specs[i].nz);
+        g.zc = tuned_zchunk(specs[i].nx, specs[i].ny, specs[i].nz, sizeof(T));
         o_cnt[i] = take(zero_bytes, g.n);
         o_req[i] = take(zero_bytes, 4 * g.nwords);
         o_a0[i] = take(zero_bytes, 4 * g.nwords);
@@ -176,7 +177,7 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
         I.stride = n;
         I.tiles_x = static_cast<uint32_t>(g.wpr);
         I.tiles_y = static_cast<uint32_t>((g.ny + kTY - 1) / kTY);
-        const uint64_t tz = static_cast<uint64_t>((g.nz + kZChunk - 1) / kZChunk);
+        const uint64_t tz = static_cast<uint64_t>((g.nz + g.zc - 1) / g.zc);
         tpre[i] = static_cast<uint32_t>(tiles);
         rpre[i] = static_cast<uint32_t>(rounds);
         tiles += static_cast<uint64_t>(I.tiles_x) * I.tiles_y * tz;
@@ -339,8 +340,14 @@ int batch_impl(const std::vector<FieldSpec<T>> &specs, const pmsz_opts *opts, st
     const int q = opts ? opts->q : 5;
     const int64_t max_sweeps = opts && opts->max_sweeps > 0 ? opts->max_sweeps : 10000;
     if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
+    int rc = PMSZ_OK;
+    if (opts && (opts->flags & PMSZ_FLAG_AUTOTUNE))  // the first field of each untuned shape class tunes it
+        for (const FieldSpec<T> &sp : specs)
+            if (!tune_known(sp.nx, sp.ny, sp.nz, sizeof(T)) &&
+                (rc = autotune_impl<T>(sp.f, sp.fh, sp.nx, sp.ny, sp.nz, nullptr, s)))
+                return rc;
     MultiRun<T> run(s);
-    int rc = run.setup(specs, max_sweeps, q, s);
+    rc = run.setup(specs, max_sweeps, q, s);
     if (rc) return rc;
     const int n = run.n;
     out.assign(n, BatchOutcome{});

@@ -164,7 +164,10 @@ struct Geom {
     size_t nwords;    // wpr * ny * nz (< 2^32)
     size_t n;         // nx * ny * nz
     FastDiv div_wpr, div_ny, div_nx;  // div_nx: for flat indices below 2^32
+    int zc;           // planes per tile column of the tiled passes (tile 32 x 8 x zc)
 };
+
+constexpr int kZChunkDefault = 32;  // zc when no tuned value is recorded for the shape
 
 inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
     Geom g;
@@ -177,6 +180,7 @@ inline Geom make_geom(size_t nx, size_t ny, size_t nz) {
     g.div_wpr = make_fastdiv(static_cast<uint32_t>(g.wpr));
     g.div_ny = make_fastdiv(static_cast<uint32_t>(ny));
     g.div_nx = make_fastdiv(static_cast<uint32_t>(nx));
+    g.zc = kZChunkDefault;
     return g;
 }
 

@@ -270,8 +270,8 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
                       uint32_t *xlist, uint32_t *xcount) {
     if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
-    const int nchunks = (g.nz + kZChunk - 1) / kZChunk;
-    const size_t chunk_bytes = 2 * plane * kZChunk * sizeof(T);
+    const int nchunks = (g.nz + g.zc - 1) / g.zc;
+    const size_t chunk_bytes = 2 * plane * static_cast<size_t>(g.zc) * sizeof(T);
     const int cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
     const int nslabs = (nchunks + cps - 1) / cps;
     // cs: host copies; ds: device copies of fhat into dprev (kept off cs so
@@ -296,8 +296,8 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
     PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
     PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
     for (int j = 0; j < nslabs; ++j) {
-        const size_t z0 = static_cast<size_t>(j) * cps * kZChunk;
-        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * kZChunk);
+        const size_t z0 = static_cast<size_t>(j) * cps * g.zc;
+        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * g.zc);
         const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
         PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
         PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
@@ -336,7 +336,11 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const int64_t max_sweeps = opts && opts->max_sweeps > 0 ? opts->max_sweeps : 10000;
     if (!(eb > 0.0) || !(eb < 1e300)) return set_error(PMSZ_ERR_ARG, "error bound must be positive and finite");
     if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
-    const Geom g = make_geom(nx, ny, nz);
+    if ((flags & PMSZ_FLAG_AUTOTUNE) && !ingest && !tune_known(nx, ny, nz, sizeof(T)) &&
+        (rc = autotune_impl<T>(f, fh, nx, ny, nz, nullptr, s)))
+        return rc;
+    Geom g = make_geom(nx, ny, nz);
+    g.zc = tuned_zchunk(nx, ny, nz, sizeof(T));
     const T eps = static_cast<T>(eb);
     const T delta = static_cast<T>(eb / static_cast<double>(q));  // pMSz.cu:2814
 
@@ -629,6 +633,62 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
     PMSZ_CUDA(cudaGetLastError());
     return PMSZ_OK;
 }
+
+// The tuner's first-pass timing: the fused first pass (deferring form) of
+// f / fhat at each tile depth zcs[k] on scratch of its own; ms[k] is the best
+// of two timed launches after a warm-up.  The code bytes (independent of the
+// depth) go to the caller's buffer, completed by k_first_exact for the voxels
+// the last run deferred, so every byte is a valid pair of ranks.
+template <typename T>
+int time_first_pass(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, uint8_t *codes, const int *zcs, int m,
+                    float *ms, cudaStream_t s) {
+    Geom g = make_geom(nx, ny, nz);
+    const bool defer = g.n < (static_cast<size_t>(1) << 32);
+    Workspace ws(s);
+    const size_t o_hp = ws.reserve<uint32_t>(g.n), o_req = ws.reserve<uint32_t>(g.nwords),
+                 o_act = ws.reserve<uint32_t>(g.nwords), o_slot = ws.reserve<SweepSlot>(1),
+                 o_x = ws.reserve<uint32_t>(defer ? g.n : 0), o_xc = ws.reserve<uint32_t>(1);
+    int rc = ws.commit();
+    if (rc) return rc;
+    uint32_t *hp = ws.at<uint32_t>(o_hp), *req = ws.at<uint32_t>(o_req), *act = ws.at<uint32_t>(o_act);
+    uint32_t *xl = ws.at<uint32_t>(o_x), *xc = ws.at<uint32_t>(o_xc);
+    SweepSlot *slot = ws.at<SweepSlot>(o_slot);
+    EventTimer et;
+    if ((rc = et.init())) return rc;
+    const dim3 blk3(kTX, kTY, 1);
+    for (int k = 0; k < m; ++k) {
+        g.zc = zcs[k];
+        float best = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {  // the first run of each candidate is a warm-up
+            PMSZ_CUDA(cudaMemsetAsync(req, 0, g.nwords * 4, s));
+            PMSZ_CUDA(cudaMemsetAsync(act, 0, g.nwords * 4, s));
+            PMSZ_CUDA(cudaMemsetAsync(slot, 0, sizeof(SweepSlot), s));
+            PMSZ_CUDA(cudaMemsetAsync(xc, 0, sizeof(uint32_t), s));
+            PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+            if (defer)
+                k_tiled<T, kFirst, true><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act, slot, g, 0, xl, xc);
+            else
+                k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act, slot, g, 0);
+            PMSZ_CUDA(cudaGetLastError());
+            PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
+            PMSZ_CUDA(cudaEventSynchronize(et.ev[1]));
+            float t = 0.f;
+            PMSZ_CUDA(cudaEventElapsedTime(&t, et.ev[0], et.ev[1]));
+            if (rep > 0 && (best == 0.f || t < best)) best = t;
+        }
+        ms[k] = best;
+    }
+    if (defer) {  // the deferred voxels' code bytes: codes is complete for the caller
+        k_first_exact<T><<<152 * 8, 256, 0, s>>>(xl, xc, f, fh, codes, req, act, slot, g, g.div_nx);
+        PMSZ_CUDA(cudaGetLastError());
+    }
+    return ws.release();
+}
+
+template int time_first_pass<float>(const float *, const float *, size_t, size_t, size_t, uint8_t *, const int *, int,
+                                    float *, cudaStream_t);
+template int time_first_pass<double>(const double *, const double *, size_t, size_t, size_t, uint8_t *, const int *,
+                                     int, float *, cudaStream_t);
 
 template int codes_impl<float>(const float *, size_t, size_t, size_t, uint8_t *, cudaStream_t);
 template int codes_impl<double>(const double *, size_t, size_t, size_t, uint8_t *, cudaStream_t);

@@ -111,6 +111,22 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
 // AS / DS labels (roots of the steepest-ascent / descent forests) of a code
 // array; n < 2^32.
 int labels_impl(const uint8_t *codes, size_t nx, size_t ny, size_t nz, uint32_t *as, uint32_t *ds, cudaStream_t s);
+// Tuning table (tune.cu): the tile depth (planes per tile column) and the
+// pointer-jumping rounds per launch recorded for a shape class, or the
+// defaults; tune_known says whether the class has an entry.
+int tuned_zchunk(size_t nx, size_t ny, size_t nz, size_t elem);
+int tuned_jump_rounds(size_t nx, size_t ny, size_t nz);
+bool tune_known(size_t nx, size_t ny, size_t nz, size_t elem);
+template <typename T>
+int autotune_impl(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, pmsz_tune *out, cudaStream_t s);
+// The tuner's measurements: the fused first pass at each tile depth
+// (correct.cu), and the AS labels of a code array at each rounds-per-launch
+// count (verify.cu).
+template <typename T>
+int time_first_pass(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, uint8_t *codes, const int *zcs, int m,
+                    float *ms, cudaStream_t s);
+int time_jump_rounds(const uint8_t *codes, size_t nx, size_t ny, size_t nz, const int *rounds, int m, float *ms,
+                     cudaStream_t s);
 template <typename T>
 int naive_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
                pmsz_result *res, cudaStream_t s);

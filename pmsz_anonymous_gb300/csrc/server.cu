@@ -120,6 +120,7 @@ public:
         auto j = std::make_unique<Job>();
         j->fd = fd;
         j->g = make_geom(fd.nx, fd.ny, fd.nz);
+        j->g.zc = tuned_zchunk(fd.nx, fd.ny, fd.nz, fd.elem_size);
         j->scratch_bytes = field_scratch_bytes(j->g, cfg_.max_sweeps);
         // its fields, its scratch, and its share of the group's voxel lists
         j->bytes = j->scratch_bytes + 2 * j->g.n * fd.elem_size + 2 * sizeof(uint64_t) * j->g.n;
@@ -247,7 +248,7 @@ private:
             any_first |= j.first;
             pre[i] = static_cast<uint32_t>(tiles);
             pre[n + 1 + i] = static_cast<uint32_t>(rounds);
-            tiles += static_cast<uint64_t>(G.host[i].tiles_x) * G.host[i].tiles_y * ((j.g.nz + kZChunk - 1) / kZChunk);
+            tiles += static_cast<uint64_t>(G.host[i].tiles_x) * G.host[i].tiles_y * ((j.g.nz + j.g.zc - 1) / j.g.zc);
             rounds += (j.g.nwords + kRoundWords - 1) / kRoundWords;
         }
         if (tiles >= (1ull << 31) || rounds >= (1ull << 31)) return set_error(PMSZ_ERR_ARG, "running set too large");

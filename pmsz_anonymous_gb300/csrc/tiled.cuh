@@ -78,7 +78,7 @@ __device__ __forceinline__ Ext proxy_ext_interior(const uint32_t (&t)[15]) {
     return e;
 }
 
-constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kRing = 4, kZChunk = 32;
+constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kRing = 4;
 constexpr int kCells = kHX * kHY, kThreads = kTX * kTY;
 enum TileMode { kFirst = 0, kDetect = 1, kCodes = 2 };
 
@@ -104,7 +104,7 @@ __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; 
 
 // ---------------------------------------------------------------------------
 // Tiled full-field pass.  Block (32, 8) owns a 32x8 column of the field and
-// marches it through kZChunk planes; planes (with a one-voxel halo) stream
+// marches it through g.zc planes; planes (with a one-voxel halo) stream
 // through a 4-slot ring in shared memory, prefetched two planes ahead, one
 // barrier per plane.  Each thread loads the same (at most two) cells of every
 // plane, so their coordinates are decoded once per block.
@@ -131,7 +131,7 @@ __device__ __forceinline__ void tiled_body(TileSmem<T, MODE == kFirst ? 2 : 1, !
     using K = typename KeyOf<T>::type;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
     const int x0 = bx * kTX, y0 = by * kTY;
-    const int zb = bz * kZChunk, ze = min(g.nz, zb + kZChunk);
+    const int zb = bz * g.zc, ze = min(g.nz, zb + g.zc);
     const int x = x0 + tx, y = y0 + ty;
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
 
@@ -599,7 +599,7 @@ __host__ __device__ __forceinline__ bool sweep_stops(unsigned long long fmax, un
 
 inline dim3 tiled_grid(const Geom &g) {
     return dim3(static_cast<unsigned>(g.wpr), static_cast<unsigned>((g.ny + kTY - 1) / kTY),
-                static_cast<unsigned>((g.nz + kZChunk - 1) / kZChunk));
+                static_cast<unsigned>((g.nz + g.zc - 1) / g.zc));
 }
 
 }  // namespace pmsz

@@ -5,7 +5,10 @@
 // replaces L[i] by L[L[L[i]]] in place (a vertex's pointer only ever moves to
 // another vertex of its own chain, so concurrent readers see valid ancestors)
 // and the rounds stop when one changes nothing: O(log path length) rounds of
-// coalesced work instead of one unbounded walk per thread.
+// coalesced work instead of one unbounded walk per thread.  A launch gives
+// every vertex up to `rounds` such jumps (the tuned pointer-jumping rounds per
+// launch) before the host reads the convergence flag; a launch that changes
+// nothing reads a static array, so it certifies the fixpoint.
 //
 // Verification replaces the reference's disabled check_consistency block
 // (pMSz.cu:3038-3126) and count_false_cases (pMSz.cu:1852-1870).
@@ -29,16 +32,22 @@ __global__ void __launch_bounds__(256) k_init_ptr(const uint8_t *__restrict__ co
     if (ds) ds[i] = static_cast<uint32_t>(flat(g, x + rank_dx(d), y + rank_dy(d), z + rank_dz(d)));
 }
 
-__global__ void __launch_bounds__(256) k_jump(uint32_t *__restrict__ L, size_t n, unsigned int *changed) {
+__global__ void __launch_bounds__(256) k_jump(uint32_t *__restrict__ L, size_t n, unsigned int *changed,
+                                              int rounds) {
     bool any = false;
     const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
     for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t l = L[i];
-        const uint32_t ll = L[l];
-        if (ll != l) {
+        uint32_t l = L[i];
+        bool moved = false;
+        for (int r = 0; r < rounds; ++r) {
+            const uint32_t ll = L[l];
+            if (ll == l) break;
             // three hops: a pointer spanning d chain steps now spans at least 3d
-            const uint32_t lll = L[ll];
-            L[i] = lll;
+            l = L[ll];
+            moved = true;
+        }
+        if (moved) {
+            L[i] = l;
             any = true;
         }
     }
@@ -49,12 +58,12 @@ static inline unsigned grid_for(size_t n) {
     return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16)));
 }
 
-static int jump_to_roots(uint32_t *L, size_t n, unsigned int *d_flag, cudaStream_t s) {
+static int jump_to_roots(uint32_t *L, size_t n, unsigned int *d_flag, cudaStream_t s, int rounds) {
     unsigned int *h = static_cast<unsigned int *>(host_pinned(sizeof(unsigned int)));
     if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
-    for (int round = 0; round < 64; ++round) {
+    for (int launch = 0; launch < 64; ++launch) {
         PMSZ_CUDA(cudaMemsetAsync(d_flag, 0, sizeof(unsigned int), s));
-        k_jump<<<grid_for(n), 256, 0, s>>>(L, n, d_flag);
+        k_jump<<<grid_for(n), 256, 0, s>>>(L, n, d_flag, rounds);
         PMSZ_CUDA(cudaGetLastError());
         PMSZ_CUDA(cudaMemcpyAsync(h, d_flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         PMSZ_CUDA(cudaStreamSynchronize(s));
@@ -75,8 +84,39 @@ int labels_impl(const uint8_t *codes, size_t nx, size_t ny, size_t nz, uint32_t 
     const dim3 grid(static_cast<unsigned>(g.wpr), static_cast<unsigned>((g.ny + 7) / 8), static_cast<unsigned>(g.nz));
     k_init_ptr<<<grid, dim3(32, 8, 1), 0, s>>>(codes, as, ds, g);
     PMSZ_CUDA(cudaGetLastError());
-    if (as && (rc = jump_to_roots(as, g.n, ws.at<unsigned int>(o_flag), s))) return rc;
-    if (ds && (rc = jump_to_roots(ds, g.n, ws.at<unsigned int>(o_flag), s))) return rc;
+    const int rounds = tuned_jump_rounds(nx, ny, nz);
+    if (as && (rc = jump_to_roots(as, g.n, ws.at<unsigned int>(o_flag), s, rounds))) return rc;
+    if (ds && (rc = jump_to_roots(ds, g.n, ws.at<unsigned int>(o_flag), s, rounds))) return rc;
+    return ws.release();
+}
+
+int time_jump_rounds(const uint8_t *codes, size_t nx, size_t ny, size_t nz, const int *rounds, int m, float *ms,
+                     cudaStream_t s) {
+    const Geom g = make_geom(nx, ny, nz);
+    for (int k = 0; k < m; ++k) ms[k] = 0.f;
+    if (g.n >= (static_cast<size_t>(1) << 32)) return PMSZ_OK;  // no labels at this size
+    Workspace ws(s);
+    const size_t o_l = ws.reserve<uint32_t>(g.n), o_flag = ws.reserve<unsigned int>(1);
+    int rc = ws.commit();
+    if (rc) return rc;
+    uint32_t *L = ws.at<uint32_t>(o_l);
+    EventTimer et;
+    if ((rc = et.init())) return rc;
+    const dim3 grid(static_cast<unsigned>(g.wpr), static_cast<unsigned>((g.ny + 7) / 8), static_cast<unsigned>(g.nz));
+    for (int k = 0; k < m; ++k) {
+        float best = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {  // the first run of each candidate is a warm-up
+            k_init_ptr<<<grid, dim3(32, 8, 1), 0, s>>>(codes, L, nullptr, g);
+            PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+            if ((rc = jump_to_roots(L, g.n, ws.at<unsigned int>(o_flag), s, rounds[k]))) return rc;
+            PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
+            PMSZ_CUDA(cudaEventSynchronize(et.ev[1]));
+            float t = 0.f;
+            PMSZ_CUDA(cudaEventElapsedTime(&t, et.ev[0], et.ev[1]));
+            if (rep > 0 && (best == 0.f || t < best)) best = t;
+        }
+        ms[k] = best;
+    }
     return ws.release();
 }
 

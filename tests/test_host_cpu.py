@@ -1,5 +1,6 @@
 """CPU tests of the native library that need no GPU: it loads, exports every
 symbol the headers declare, and its host encoder matches the oracle."""
+import ctypes
 import os
 import re
 
@@ -93,3 +94,50 @@ def test_fields_are_normalised_and_bounded():
         fh = F.standin(f, 1e-3, comp)
         assert np.all(np.abs(f - fh) <= np.float32(1e-3))
     assert np.array_equal(F.perlin_field((4, 5, 6), 3, 2, 0.1), F.perlin_field((4, 5, 6), 3, 2, 0.1))
+
+
+def _tune(lib, shape, elem):
+    t = capi.Tune()
+    nz, ny, nx = shape
+    return lib.pmsz_tune_get(nx, ny, nz, elem, ctypes.byref(t)), t
+
+
+def test_tuning_table_round_trip_without_gpu(lib, tmp_path):
+    lib.pmsz_tune_clear()
+    try:
+        found, t = _tune(lib, (64, 64, 64), 8)
+        assert found == 0 and (t.zchunk, t.jump_rounds) == (32, 1)  # defaults
+        assert lib.pmsz_tune_set(64, 64, 64, 8, ctypes.byref(capi.Tune(16, 4))) == capi.PMSZ_OK
+        found, t = _tune(lib, (33, 50, 61), 8)  # same ceil-log2 class as 64^3
+        assert found == 1 and (t.zchunk, t.jump_rounds) == (16, 4)
+        found, t = _tune(lib, (64, 64, 64), 4)  # the tile depth is per element size; rounds are not
+        assert found == 0 and (t.zchunk, t.jump_rounds) == (32, 4)
+        assert lib.pmsz_tune_set(300, 20, 7, 4, ctypes.byref(capi.Tune(64, 2))) == capi.PMSZ_OK
+        path = str(tmp_path / "tune.txt")
+        assert lib.pmsz_tune_save(path.encode()) == capi.PMSZ_OK
+        text = open(path).read().splitlines()
+        assert text[0] == "pmsz-tune 1" and len(text) == 3
+        lib.pmsz_tune_clear()
+        assert _tune(lib, (64, 64, 64), 8)[0] == 0
+        assert lib.pmsz_tune_load(path.encode()) == capi.PMSZ_OK
+        found, t = _tune(lib, (64, 64, 64), 8)
+        assert found == 1 and (t.zchunk, t.jump_rounds) == (16, 4)
+        found, t = _tune(lib, (7, 20, 300), 4)
+        assert found == 1 and (t.zchunk, t.jump_rounds) == (64, 2)
+    finally:
+        lib.pmsz_tune_clear()
+
+
+def test_tuning_table_rejects_bad_entries(lib, tmp_path):
+    bad = [capi.Tune(0, 1), capi.Tune(300, 1), capi.Tune(32, 0), capi.Tune(32, 17)]
+    for t in bad:
+        assert lib.pmsz_tune_set(8, 8, 8, 4, ctypes.byref(t)) == capi.PMSZ_ERR_ARG
+    assert lib.pmsz_tune_set(8, 8, 8, 2, ctypes.byref(capi.Tune(32, 1))) == capi.PMSZ_ERR_ARG
+    assert lib.pmsz_tune_get(8, 8, 8, 3, ctypes.byref(capi.Tune())) < 0
+    p = tmp_path / "bad.txt"
+    p.write_text("pmsz-tune 1\n4 3 3 3 0 1\n")
+    assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
+    p.write_text("something else\n")
+    assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
+    assert lib.pmsz_tune_load(str(tmp_path / "missing.txt").encode()) == capi.PMSZ_ERR_IO
+    assert lib.pmsz_tune_get(8, 8, 8, 4, ctypes.byref(capi.Tune())) == 0  # nothing was recorded
