@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256, 4) k_detect_list_multi(const Inst<T> *__r
                     const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
                     t[r] = ((valid >> r) & 1u) ? __ldg(c0p + off) : 0u;
                 }
-                const Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
+                const Ext ex = interior ? proxy_ext_interior<true>(t) : proxy_ext<true>(t);
                 if (ex.exact) detect_outcome(g, x, y, z, ex.asc, ex.desc, c, I.req, nxt, w[0], w[1], w[2]);
                 else s_x[atomicAdd(&s_n, 1u)] = ent;  // at most kMultiChunk per step: no overflow
             }

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
             t[r] = ((valid >> r) & 1u) ? __ldg(c0 + off) : 0u;
         }
         const uint8_t c = __ldg(codes + i);
-        const Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
+        const Ext ex = interior ? proxy_ext_interior<true>(t) : proxy_ext<true>(t);
         ++active;
         if (ex.exact) {
             detect_outcome(g, x, y, z, ex.asc, ex.desc, c, req, act_next, cmax, cmin, cdir);

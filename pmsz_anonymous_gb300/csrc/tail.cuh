@@ -206,7 +206,7 @@ struct TailDetect {
             const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
             t[r] = ((valid >> r) & 1u) ? __ldcg(hp + (static_cast<ptrdiff_t>(i) + off)) : 0u;
         }
-        Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
+        Ext ex = interior ? proxy_ext_interior<true>(t) : proxy_ext<true>(t);
         if (!ex.exact) {
             typename KeyOf<T>::type kk[15];
 #pragma unroll

@@ -43,14 +43,28 @@ struct Ext {
 // Packed argmax / argmin of 15 proxies in rank order, with certificates.
 // General form: out-of-domain candidates carry proxy 0; the min chains add
 // -16 (and -1) so those wrap to the top of the range and lose.
+// FUSED: each chain step is one fused add-and-max / add-and-min
+// (__viaddmax_u32 / __viaddmin_u32: max(a + b, c), min(a + b, c), 32-bit
+// wrapping add) -- fewer instructions, for the latency-bound gather kernels;
+// the tiled passes, bound by the ALU pipe, keep separate adds and min/max.
+template <bool FUSED = false>
 __device__ __forceinline__ Ext proxy_ext(const uint32_t (&t)[15]) {
     uint32_t M = t[0], M2 = t[0] + 15u, m = t[0] - 16u, m2 = t[0] - 1u;
 #pragma unroll
     for (int r = 1; r < 15; ++r) {
-        M = max(M, t[r] + static_cast<uint32_t>(r));
-        M2 = max(M2, t[r] + static_cast<uint32_t>(15 - r));
-        m = min(m, t[r] + (static_cast<uint32_t>(r) - 16u));
-        m2 = min(m2, t[r] + (0u - 1u - static_cast<uint32_t>(r)));
+        const uint32_t ra = static_cast<uint32_t>(r), rb = static_cast<uint32_t>(15 - r);
+        const uint32_t rc = static_cast<uint32_t>(r) - 16u, rd = 0u - 1u - static_cast<uint32_t>(r);
+        if (FUSED) {
+            M = __viaddmax_u32(t[r], ra, M);
+            M2 = __viaddmax_u32(t[r], rb, M2);
+            m = __viaddmin_u32(t[r], rc, m);
+            m2 = __viaddmin_u32(t[r], rd, m2);
+        } else {
+            M = max(M, t[r] + ra);
+            M2 = max(M2, t[r] + rb);
+            m = min(m, t[r] + rc);
+            m2 = min(m2, t[r] + rd);
+        }
     }
     Ext e;
     e.asc = static_cast<int>(M & 15u);
@@ -61,15 +75,23 @@ __device__ __forceinline__ Ext proxy_ext(const uint32_t (&t)[15]) {
 
 // Interior form (all 15 candidates inside the domain): the max and min chains
 // share the packed values t + r and t + (15 - r), half the adds.
+template <bool FUSED = false>
 __device__ __forceinline__ Ext proxy_ext_interior(const uint32_t (&t)[15]) {
     uint32_t M = t[0], m = t[0], M2 = t[0] + 15u, m2 = M2;
 #pragma unroll
     for (int r = 1; r < 15; ++r) {
-        const uint32_t a = t[r] + static_cast<uint32_t>(r), b = t[r] + static_cast<uint32_t>(15 - r);
-        M = max(M, a);
-        m = min(m, a);
-        M2 = max(M2, b);
-        m2 = min(m2, b);
+        if (FUSED) {
+            M = __viaddmax_u32(t[r], static_cast<uint32_t>(r), M);
+            m = __viaddmin_u32(t[r], static_cast<uint32_t>(r), m);
+            M2 = __viaddmax_u32(t[r], static_cast<uint32_t>(15 - r), M2);
+            m2 = __viaddmin_u32(t[r], static_cast<uint32_t>(15 - r), m2);
+        } else {
+            const uint32_t a = t[r] + static_cast<uint32_t>(r), b = t[r] + static_cast<uint32_t>(15 - r);
+            M = max(M, a);
+            m = min(m, a);
+            M2 = max(M2, b);
+            m2 = min(m2, b);
+        }
     }
     Ext e;
     e.asc = static_cast<int>(M & 15u);
@@ -453,7 +475,7 @@ struct DetectWork {
             const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
             t[r] = ((valid >> r) & 1u) ? L::ld(c0 + off) : 0u;
         }
-        Ext ex = interior ? proxy_ext_interior(t) : proxy_ext(t);
+        Ext ex = interior ? proxy_ext_interior<true>(t) : proxy_ext<true>(t);
         if (!ex.exact) {
             typename KeyOf<T>::type kk[15];
 #pragma unroll
