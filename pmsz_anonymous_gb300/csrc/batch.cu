@@ -34,7 +34,7 @@ __device__ __forceinline__ int find_seg(const uint32_t *__restrict__ pre, int n,
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 5) k_first_multi(const Inst<T> *__restrict__ inst,
                                                             const uint32_t *__restrict__ tpre, int n) {
-    __shared__ TileSmem<T, 2, true> sm;
+    __shared__ TileOf<T, kFirst, false> sm;
     const int i = find_seg(tpre, n, blockIdx.x);
     const Inst<T> &I = inst[i];
     if (!I.first) return;  // uniform: only fields that start now
@@ -205,6 +205,7 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
     const size_t o_list = ws.reserve<uint64_t>(lists ? total_voxels : 0);
     const size_t o_xlist = ws.reserve<uint64_t>(lists ? total_voxels : 0);
     const size_t o_lc = ws.reserve<uint32_t>(lists ? 4 : 0);
+    const size_t o_state = ws.reserve<BatchState>(lists ? 1 : 0);
     int rc = ws.commit();
     if (rc) return rc;
     if (lists) {
@@ -213,6 +214,7 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
         ml.list = ws.at<uint64_t>(o_list);
         ml.xlist = ws.at<uint64_t>(o_xlist);
         ml.lc = ws.at<uint32_t>(o_lc);
+        ml.state = ws.at<BatchState>(o_state);
         PMSZ_CUDA(cudaMemcpyAsync(ml.wpre, wpre.data(), wpre.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     }
     unsigned char *zero = ws.at<unsigned char>(o_zero), *other = ws.at<unsigned char>(o_other);
@@ -240,8 +242,20 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
 
 template <typename T>
 int MultiRun<T>::push_table() {
-    PMSZ_CUDA(cudaMemcpyAsync(dinst, host.data(), host.size() * sizeof(Inst<T>), cudaMemcpyHostToDevice, s));
-    // the host copy may be rewritten right after: wait for the copy
+    if (!pin) PMSZ_CUDA(cudaMallocHost(reinterpret_cast<void **>(&pin), 2 * host.size() * sizeof(Inst<T>)));
+    Inst<T> *dst = pin + static_cast<size_t>(pin_next) * host.size();
+    pin_next ^= 1;
+    std::copy(host.begin(), host.end(), dst);
+    PMSZ_CUDA(cudaMemcpyAsync(dinst, dst, host.size() * sizeof(Inst<T>), cudaMemcpyHostToDevice, s));
+    return PMSZ_OK;
+}
+
+template <typename T>
+int MultiRun<T>::read_rows(int64_t k, int64_t count, std::vector<SweepSlot> &out) {
+    out.resize(static_cast<size_t>(count) * n);
+    if (count > 0)
+        PMSZ_CUDA(cudaMemcpyAsync(out.data(), slots + k * n, out.size() * sizeof(SweepSlot), cudaMemcpyDeviceToHost,
+                                  s));
     PMSZ_CUDA(cudaStreamSynchronize(s));
     return PMSZ_OK;
 }
@@ -332,6 +346,90 @@ int MultiRun<T>::loop(int64_t *iters) {
 template struct MultiRun<float>;
 template struct MultiRun<double>;
 
+// The list form of a batch: generation 0 (first passes and the first edits)
+// on the stream, then the generations as a CUDA graph whose while node
+// repeats one generation and k_batch_gate until the gate stops it -- no host
+// round trip per generation; the graph is built while generation 0 runs.
+// What the gate leaves (small active sets) goes to the cooperative tail.  The
+// sweep logs and statuses are rebuilt afterwards from the slot rows, with the
+// stop rule the gate and the tail applied.
+template <typename T>
+static int run_gated(MultiRun<T> &run, int64_t max_sweeps, std::vector<BatchOutcome> &out) {
+    const int n = run.n;
+    cudaStream_t s = run.s;
+    size_t total_n = 0;
+    for (const Inst<T> &I : run.host) total_n += I.g.n;
+    const unsigned long long tail_at = std::max<unsigned long long>(total_n / 32, 1ull << 16);
+    BatchState *st = run.ml.state;
+    PMSZ_CUDA(cudaMemsetAsync(st, 0, sizeof(BatchState), s));
+    PMSZ_CUDA(cudaMemsetAsync(&st->go, 1, 1, s));  // generation 0 runs (little-endian int 1)
+    int rc = run.generation();
+    if (rc) return rc;
+    k_batch_gate<T><<<1, 256, 0, s>>>(run.dinst, n, st, max_sweeps, tail_at, cudaGraphConditionalHandle{}, 0);
+    PMSZ_CUDA(cudaGetLastError());
+
+    struct GraphGuard {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaStream_t cs = nullptr;
+        ~GraphGuard() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } gg;
+    PMSZ_CUDA(cudaGraphCreate(&gg.graph, 0));
+    cudaGraphConditionalHandle cond;
+    PMSZ_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
+    PMSZ_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    // the body runs once even when generation 0's gate stopped: its kernels
+    // then see go == 0 and return at once
+    if ((rc = launch_list_sweep<T>(run.dinst, n, run.ml, gg.cs, &st->go))) {
+        cudaStreamEndCapture(gg.cs, &body);
+        return rc;
+    }
+    k_batch_gate<T><<<1, 256, 0, gg.cs>>>(run.dinst, n, st, max_sweeps, tail_at, cond, 1);
+    PMSZ_CUDA(cudaStreamEndCapture(gg.cs, &body));
+    PMSZ_CUDA(cudaGraphInstantiate(&gg.exec, gg.graph, 0));
+    PMSZ_CUDA(cudaGraphLaunch(gg.exec, s));
+
+    BatchState hs;
+    PMSZ_CUDA(cudaMemcpyAsync(&hs, st, sizeof(BatchState), cudaMemcpyDeviceToHost, s));
+    PMSZ_CUDA(cudaStreamSynchronize(s));
+    int64_t total = hs.k;  // sweeps 0 .. total-1 ran as generations
+    if (hs.live > 0) {     // the rest of the live fields in the cooperative tail
+        PMSZ_CUDA(cudaMemcpyAsync(run.host.data(), run.dinst, n * sizeof(Inst<T>), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        int64_t iters = 0;
+        if ((rc = run.loop(&iters))) return rc;
+        total += iters;
+    }
+    std::vector<SweepSlot> rows;
+    if ((rc = run.read_rows(0, total, rows))) return rc;
+    for (int i = 0; i < n; ++i) {
+        for (int64_t k = 0; k < total; ++k) {
+            const SweepSlot &h = rows[static_cast<size_t>(k) * n + i];
+            out[i].log.push_back(h);
+            if (k == 0 && h.bad) {
+                out[i].status = PMSZ_ERR_ARG;
+                out[i].message = "input contains NaN or the value 1e30 (the reference's halo sentinel)";
+                break;
+            }
+            if (sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + 1, max_sweeps)) break;
+        }
+    }
+    return PMSZ_OK;
+}
+
 // Corrects a batch of same-type fields: first pass, host-driven sweeps while
 // the batch's next active sets are large, then the cooperative tail loop.
 template <typename T>
@@ -356,57 +454,60 @@ int batch_impl(const std::vector<FieldSpec<T>> &specs, const pmsz_opts *opts, st
         I.first = 1;
         I.k = 0;
     }
-    if ((rc = run.generation())) return rc;
-    std::vector<SweepSlot> row;
-    int64_t k = 0;
-    size_t total_n = 0;
-    for (const Inst<T> &I : run.host) total_n += I.g.n;
-    // decisions after each host-driven sweep
-    while (true) {
-        if ((rc = run.read_row(k, row))) return rc;
-        unsigned long long est = 0;
-        int live = 0;
-        for (int i = 0; i < n; ++i) {
-            Inst<T> &I = run.host[i];
-            if (!I.active) continue;
-            const SweepSlot &h = row[i];
-            out[i].log.push_back(h);
-            if (k == 0 && h.bad) {
-                I.active = 0;
-                out[i].status = PMSZ_ERR_ARG;
-                out[i].message = "input contains NaN or the value 1e30 (the reference's halo sentinel)";
-                continue;
-            }
-            if (sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + 1, max_sweeps)) {
-                I.active = 0;
-                continue;
-            }
-            I.k = k + 1;
-            est += 15ull * h.changed + h.fdir;
-            ++live;
-        }
-        ++k;
-        if (!live) break;
-        if (est <= std::max<unsigned long long>(total_n / 32, 1ull << 16)) {
-            int64_t iters = 0;
-            if ((rc = run.loop(&iters))) return rc;
-            // rebuild each live field's tail from the slot rows
-            std::vector<std::vector<SweepSlot>> rows(iters);
-            for (int64_t j = 0; j < iters; ++j)
-                if ((rc = run.read_row(k + j, rows[j]))) return rc;
+    if (run.lists) {
+        if ((rc = run_gated<T>(run, max_sweeps, out))) return rc;
+    } else {
+        if ((rc = run.generation())) return rc;
+        std::vector<SweepSlot> row;
+        int64_t k = 0;
+        size_t total_n = 0;
+        for (const Inst<T> &I : run.host) total_n += I.g.n;
+        // decisions after each host-driven sweep
+        while (true) {
+            if ((rc = run.read_row(k, row))) return rc;
+            unsigned long long est = 0;
+            int live = 0;
             for (int i = 0; i < n; ++i) {
                 Inst<T> &I = run.host[i];
                 if (!I.active) continue;
-                for (int64_t j = 0; j < iters; ++j) {
-                    const SweepSlot &h = rows[j][i];
-                    out[i].log.push_back(h);
-                    if (sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + j + 1, max_sweeps)) break;
+                const SweepSlot &h = row[i];
+                out[i].log.push_back(h);
+                if (k == 0 && h.bad) {
+                    I.active = 0;
+                    out[i].status = PMSZ_ERR_ARG;
+                    out[i].message = "input contains NaN or the value 1e30 (the reference's halo sentinel)";
+                    continue;
                 }
-                I.active = 0;
+                if (sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + 1, max_sweeps)) {
+                    I.active = 0;
+                    continue;
+                }
+                I.k = k + 1;
+                est += 15ull * h.changed + h.fdir;
+                ++live;
             }
-            break;
+            ++k;
+            if (!live) break;
+            if (est <= std::max<unsigned long long>(total_n / 32, 1ull << 16)) {
+                int64_t iters = 0;
+                if ((rc = run.loop(&iters))) return rc;
+                // rebuild each live field's tail from the slot rows
+                std::vector<SweepSlot> rows;
+                if ((rc = run.read_rows(k, iters, rows))) return rc;
+                for (int i = 0; i < n; ++i) {
+                    Inst<T> &I = run.host[i];
+                    if (!I.active) continue;
+                    for (int64_t j = 0; j < iters; ++j) {
+                        const SweepSlot &h = rows[static_cast<size_t>(j) * n + i];
+                        out[i].log.push_back(h);
+                        if (sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + j + 1, max_sweeps)) break;
+                    }
+                    I.active = 0;
+                }
+                break;
+            }
+            if ((rc = run.generation())) return rc;
         }
-        if ((rc = run.generation())) return rc;
     }
     for (int i = 0; i < n; ++i) {
         BatchOutcome &o = out[i];

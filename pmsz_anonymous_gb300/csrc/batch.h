@@ -46,12 +46,21 @@ struct BatchOutcome {
 };
 
 // Scratch of the voxel-list generations of a table of fields (batch_list.cuh).
+// State of the device-gated generations of pmsz_correct_batch (k_batch_gate).
+struct BatchState {
+    long long k;             // sweep index of the next generation
+    int go;                  // the next generation runs
+    int live;                // fields still running after the last gate
+    unsigned long long est;  // their next active sets, estimated (15 * changed + fdir)
+};
+
 struct MultiLists {
     uint32_t *wpre = nullptr;   // n + 1 word prefixes (multiples of 4), device
     uint64_t total_words = 0;
     uint32_t *counts = nullptr; // one count per compaction block (kCompactBlocks)
     uint64_t *list = nullptr, *xlist = nullptr;  // capacity: the fields' voxels
     uint32_t *lc = nullptr;     // 4 list lengths
+    BatchState *state = nullptr;
 };
 
 // Scratch and table of one multi-field run; slot rows are sweep-major
@@ -59,6 +68,11 @@ struct MultiLists {
 template <typename T>
 struct MultiRun {
     explicit MultiRun(cudaStream_t st) : s(st), ws(st) {}
+    ~MultiRun() {
+        if (pin) cudaFreeHost(pin);
+    }
+    MultiRun(const MultiRun &) = delete;
+    MultiRun &operator=(const MultiRun &) = delete;
     int setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweeps, int q, cudaStream_t s);
     // One generation: the fused first pass of fields with `first` set, the
     // detection of every other active field, then the edits of all active
@@ -67,6 +81,11 @@ struct MultiRun {
     // The remaining sweeps of all active fields in one cooperative launch.
     int loop(int64_t *iters);
     int read_row(int64_t k, std::vector<SweepSlot> &row);
+    // rows k .. k+count-1 in one copy (row j at out[j * n])
+    int read_rows(int64_t k, int64_t count, std::vector<SweepSlot> &out);
+    // The host table goes up through one of two pinned copies in turn, with
+    // no wait: every generation ends in a read_row, which synchronises the
+    // stream before the same copy is written again.
     int push_table();
 
     cudaStream_t s;
@@ -82,7 +101,9 @@ struct MultiRun {
     long long *diters = nullptr;
     SweepSlot *slots = nullptr;
     MultiLists ml;
-    bool lists = false;  // voxel-list generations (all fields together below 2^32 voxels)
+    bool lists = false;
+    Inst<T> *pin = nullptr;  // 2 * n table entries, pinned
+    int pin_next = 0;  // voxel-list generations (all fields together below 2^32 voxels)
 };
 
 // One generation over a device table of n fields (see MultiRun::generation),

@@ -49,8 +49,10 @@ __host__ __device__ __forceinline__ uint64_t multi_per(uint64_t total_words) {
 template <typename T, int P>
 __global__ void __launch_bounds__(kCompactBlock) k_count_words_multi(const Inst<T> *__restrict__ inst,
                                                                      const uint32_t *__restrict__ wpre, int n,
-                                                                     uint64_t total_words, uint32_t *__restrict__ counts) {
+                                                                     uint64_t total_words, uint32_t *__restrict__ counts,
+                                                                     const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
+    if (run && *run == 0) return;
     const uint64_t per = multi_per(total_words);
     const uint64_t lo = static_cast<uint64_t>(blockIdx.x) * per, hi = min(total_words, lo + per);
     uint32_t c = 0;
@@ -70,9 +72,11 @@ __global__ void __launch_bounds__(kCompactBlock) k_write_list_multi(const Inst<T
                                                                     const uint32_t *__restrict__ wpre, int n,
                                                                     uint64_t total_words,
                                                                     const uint32_t *__restrict__ counts,
-                                                                    uint64_t *__restrict__ list, uint32_t *total) {
+                                                                    uint64_t *__restrict__ list, uint32_t *total,
+                                                                    const int *run) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
     __shared__ __align__(16) unsigned char s_raw[kStageBytes];
+    if (run && *run == 0) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint32_t before = 0, all = 0;
     for (int b = t; b < static_cast<int>(gridDim.x); b += kCompactBlock) {
@@ -157,10 +161,12 @@ __device__ __forceinline__ void multi_flush(SweepSlot *slot, const uint32_t (&v)
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_detect_list_multi(const Inst<T> *__restrict__ inst,
                                                              const uint64_t *__restrict__ list, const uint32_t *count,
-                                                             uint64_t *__restrict__ xlist, uint32_t *xcount) {
+                                                             uint64_t *__restrict__ xlist, uint32_t *xcount,
+                                                             const int *run) {
     constexpr bool kExactKeys = sizeof(T) == 4;
     __shared__ uint64_t s_x[kExactKeys ? 1 : kMultiChunk];
     __shared__ uint32_t s_n, s_base;
+    if (run && *run == 0) return;
     const uint32_t m = *count;
     for (uint32_t c0 = blockIdx.x * kMultiChunk; c0 < m; c0 += gridDim.x * kMultiChunk) {
         const uint32_t c1 = min(m, c0 + kMultiChunk);
@@ -232,7 +238,9 @@ __global__ void __launch_bounds__(256, 4) k_detect_list_multi(const Inst<T> *__r
 // almost always belongs to one field and its counters are summed per block.
 template <typename T>
 __global__ void __launch_bounds__(256) k_detect_exact_multi(const Inst<T> *__restrict__ inst,
-                                                            const uint64_t *__restrict__ xlist, const uint32_t *count) {
+                                                            const uint64_t *__restrict__ xlist, const uint32_t *count,
+                                                            const int *run) {
+    if (run && *run == 0) return;
     const uint32_t m = *count;
     using K = typename KeyOf<T>::type;
     for (uint32_t c0 = blockIdx.x * kMultiChunk; c0 < m; c0 += gridDim.x * kMultiChunk) {
@@ -283,7 +291,9 @@ __global__ void __launch_bounds__(256) k_detect_exact_multi(const Inst<T> *__res
 // closed stencil of the whole word once (15 atomics per word, not per voxel).
 template <typename T>
 __global__ void __launch_bounds__(256) k_apply_list_multi(const Inst<T> *__restrict__ inst,
-                                                          const uint64_t *__restrict__ list, const uint32_t *count) {
+                                                          const uint64_t *__restrict__ list, const uint32_t *count,
+                                                          const int *run) {
+    if (run && *run == 0) return;
     const uint32_t m = *count;
     const int lane = threadIdx.x & 31;
     for (uint32_t c0 = blockIdx.x * kMultiChunk; c0 < m; c0 += gridDim.x * kMultiChunk) {
@@ -340,22 +350,69 @@ __global__ void __launch_bounds__(256) k_apply_list_multi(const Inst<T> *__restr
 }
 
 // Detection of every running field that does not start now, then the edits of
-// every running field, as voxel-list passes.
+// every running field, as voxel-list passes.  run: a device flag that turns
+// every kernel into a no-op when zero (the gated graph loop), or null.
 template <typename T>
-int launch_list_sweep(const Inst<T> *dinst, int n, const MultiLists &ml, cudaStream_t s) {
+int launch_list_sweep(const Inst<T> *dinst, int n, const MultiLists &ml, cudaStream_t s, const int *run = nullptr) {
     PMSZ_CUDA(cudaMemsetAsync(ml.lc, 0, 4 * sizeof(uint32_t), s));
     const unsigned blocks = 152 * 4;
-    k_count_words_multi<T, 0><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts);
+    k_count_words_multi<T, 0><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts,
+                                                                       run);
     k_write_list_multi<T, 0><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts,
-                                                                      ml.list, ml.lc);
-    k_detect_list_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.list, ml.lc, ml.xlist, ml.lc + 2);
-    k_detect_exact_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.xlist, ml.lc + 2);
-    k_count_words_multi<T, 1><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts);
+                                                                      ml.list, ml.lc, run);
+    k_detect_list_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.list, ml.lc, ml.xlist, ml.lc + 2, run);
+    k_detect_exact_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.xlist, ml.lc + 2, run);
+    k_count_words_multi<T, 1><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts,
+                                                                       run);
     k_write_list_multi<T, 1><<<kCompactBlocks, kCompactBlock, 0, s>>>(dinst, ml.wpre, n, ml.total_words, ml.counts,
-                                                                      ml.list, ml.lc + 1);
-    k_apply_list_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.list, ml.lc + 1);
+                                                                      ml.list, ml.lc + 1, run);
+    k_apply_list_multi<T><<<blocks, 256, 0, s>>>(dinst, ml.list, ml.lc + 1, run);
     PMSZ_CUDA(cudaGetLastError());
     return PMSZ_OK;
+}
+
+// After generation st->k of a batch: every running field's stop rule on its
+// slot of that sweep (NaN input at sweep 0, converged, stuck, max_sweeps), the
+// survivors advance to sweep k + 1; the next generation runs (st->go) while
+// some field runs and their estimated next active sets exceed tail_at (below
+// it the cooperative tail takes over).  In the graph body it also sets the
+// condition of the while node.  One block; table rows are the fields.
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_gate(Inst<T> *inst, int n, BatchState *st, long long max_sweeps,
+                                                    unsigned long long tail_at, cudaGraphConditionalHandle cond,
+                                                    int set_cond) {
+    __shared__ unsigned long long s_est;
+    __shared__ int s_live;
+    const int go = st->go;  // block-uniform
+    if (go) {
+        if (threadIdx.x == 0) {
+            s_est = 0;
+            s_live = 0;
+        }
+        __syncthreads();
+        const long long k = st->k;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            Inst<T> &I = inst[i];
+            if (!I.active) continue;
+            const SweepSlot h = *slot_of_k(I);
+            if ((k == 0 && h.bad) || sweep_stops(h.fmax, h.fmin, h.fdir, h.progressed, k + 1, I.max_sweeps)) {
+                I.active = 0;
+                continue;
+            }
+            I.k = k + 1;
+            I.first = 0;
+            atomicAdd(&s_est, 15ull * h.changed + h.fdir);
+            atomicAdd(&s_live, 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st->k = k + 1;
+            st->live = s_live;
+            st->est = s_est;
+            st->go = (s_live > 0 && s_est > tail_at && k + 1 < max_sweeps) ? 1 : 0;
+        }
+    }
+    if (set_cond && threadIdx.x == 0) cudaGraphSetConditional(cond, st->go ? 1u : 0u);
 }
 
 }  // namespace pmsz

@@ -73,3 +73,22 @@ def test_batch_reports_bad_field_and_finishes_the_others(cuda):
     res = A.correct_batch([(a, w, 1e-3), (b, bh, 1e-3)])
     assert res[0].status == capi.PMSZ_OK and res[1].status == capi.PMSZ_ERR_ARG
     assert torch.equal(w.view(torch.uint8), ref.view(torch.uint8))
+
+
+@pytest.mark.parametrize("max_sweeps", [1, 2, 5])
+def test_batch_stops_at_max_sweeps_like_alone(cuda, max_sweeps):
+    A = _api()
+    specs = SPECS[:3] + SPECS[4:6]
+    fields = [_make(s, dt, c, eb, 60 + k, cuda) for k, (s, dt, c, eb) in enumerate(specs)]
+    for dtype in (torch.float32, torch.float64):
+        pick = [(fld, spec) for fld, spec in zip(fields, specs) if spec[1] == dtype]
+        alone = []
+        for (f, fh0), spec in pick:
+            fh = fh0.clone()
+            alone.append((fh, A.correct(f, fh, spec[3], max_sweeps=max_sweeps)))
+        work = [fh0.clone() for (_, fh0), _ in pick]
+        res = A.correct_batch([(f, w, spec[3]) for ((f, _), spec), w in zip(pick, work)], max_sweeps=max_sweeps)
+        for k, ((fh, r), b, w) in enumerate(zip(alone, res, work)):
+            assert b.status == r.status and b.sweeps == r.sweeps <= max_sweeps, k
+            np.testing.assert_array_equal(b.log[:, :5], r.log[:, :5], err_msg=f"field {k}")
+            assert torch.equal(w.view(torch.uint8), fh.view(torch.uint8)), k
