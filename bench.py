@@ -402,8 +402,9 @@ def run_batch(args):
         api.correct_batch([(f, fh.clone(), eb) for f, fh, eb in fields], autotune=True)
         chosen = [api.tune_get(f.shape, f.dtype)[1] for f, _, _ in fields]
         classes = {tuple((int(v) - 1).bit_length() for v in f.shape) for f, _, _ in fields}
-        tune_summary = {"shape_classes": len(classes),
-                        "fields_per_zchunk": dict(collections.Counter(c["zchunk"] for c in chosen)),
+        tune_summary = {"batch_zchunk": api.tune_batch_get(nvox, len(fields), torch.float32)[1],
+                        "shape_classes": len(classes),
+                        "one_by_one_fields_per_zchunk": dict(collections.Counter(c["zchunk"] for c in chosen)),
                         "fields_per_jump_rounds": dict(collections.Counter(c["jump_rounds"] for c in chosen))}
 
     def one_by_one():

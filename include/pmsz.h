@@ -346,6 +346,11 @@ int pmsz_autotune_f64(const double *f, const double *fhat, size_t nx, size_t ny,
 /* Table entry of a shape class: returns 1 and fills *out if one is recorded,
  * else 0 and the defaults (negative: bad arguments). */
 int pmsz_tune_get(size_t nx, size_t ny, size_t nz, size_t elem_size, pmsz_tune *out);
+/* The tile depth recorded for a batch's size class (ceil log2 of its total
+ * voxels, ceil log2 of its field count, the element size): pmsz_correct_batch
+ * with PMSZ_FLAG_AUTOTUNE tunes it over the whole table, since the batch runs
+ * one first-pass launch over all its fields.  Returns as pmsz_tune_get. */
+int pmsz_tune_batch_get(size_t total_voxels, int count, size_t elem_size, pmsz_tune *out);
 /* Records an entry (zchunk in 1..256, jump_rounds in 1..16). */
 int pmsz_tune_set(size_t nx, size_t ny, size_t nz, size_t elem_size, const pmsz_tune *t);
 /* Text persistence: one line per entry; load merges into the table. */

@@ -404,6 +404,17 @@ def tune_get(shape, dtype) -> tuple:
     return bool(st), {"zchunk": d["zchunk"], "jump_rounds": d["jump_rounds"]}
 
 
+def tune_batch_get(total_voxels: int, count: int, dtype) -> tuple:
+    """(recorded, zchunk): the first-pass tile depth of a batch's size class
+    (its total voxels and field count), tuned over whole batches."""
+    t = capi.Tune()
+    st = capi.load().pmsz_tune_batch_get(int(total_voxels), int(count), torch.empty(0, dtype=dtype).element_size(),
+                                         ctypes.byref(t))
+    if st < 0:
+        capi.check(-st)
+    return bool(st), int(t.zchunk)
+
+
 def tune_set(shape, dtype, zchunk: int, jump_rounds: int) -> None:
     """Record a tile depth and rounds per launch for the shape class of shape (nz, ny, nx)."""
     nz, ny, nx = (int(v) for v in shape)

@@ -108,6 +108,7 @@ SIGNATURES = {
     "pmsz_autotune_f32": (c_int, [_P, _P, c_size, c_size, c_size, _P, _P]),
     "pmsz_autotune_f64": (c_int, [_P, _P, c_size, c_size, c_size, _P, _P]),
     "pmsz_tune_get": (c_int, [c_size, c_size, c_size, c_size, _P]),
+    "pmsz_tune_batch_get": (c_int, [c_size, c_int, c_size, _P]),
     "pmsz_tune_set": (c_int, [c_size, c_size, c_size, c_size, _P]),
     "pmsz_tune_save": (c_int, [ctypes.c_char_p]),
     "pmsz_tune_load": (c_int, [ctypes.c_char_p]),

@@ -154,9 +154,12 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
     tpre.assign(n + 1, 0);
     rpre.assign(n + 1, 0);
     uint64_t tiles = 0, rounds = 0;
+    voxels = 0;
+    for (const FieldSpec<T> &sp : specs) voxels += sp.nx * sp.ny * sp.nz;
+    const int zc = tuned_batch_zchunk(voxels, n, sizeof(T));  // one first-pass launch covers the batch
     for (int i = 0; i < n; ++i) {
         Geom g = make_geom(specs[i].nx, specs[i].ny, specs[i].nz);
-        g.zc = tuned_zchunk(specs[i].nx, specs[i].ny, specs[i].nz, sizeof(T));
+        g.zc = zc;
         o_cnt[i] = take(zero_bytes, g.n);
         o_req[i] = take(zero_bytes, 4 * g.nwords);
         o_a0[i] = take(zero_bytes, 4 * g.nwords);
@@ -233,6 +236,8 @@ int MultiRun<T>::setup(const std::vector<FieldSpec<T>> &specs, int64_t max_sweep
     dtpre = ws.at<uint32_t>(o_pre);
     drpre = dtpre + (n + 1);
     diters = ws.at<long long>(o_iters);
+    zero_base = zero;
+    zero_total = zero_bytes + slot_bytes;
     PMSZ_CUDA(cudaMemsetAsync(zero, 0, zero_bytes + slot_bytes, s));
     std::vector<uint32_t> pre(tpre);
     pre.insert(pre.end(), rpre.begin(), rpre.end());
@@ -247,6 +252,66 @@ int MultiRun<T>::push_table() {
     pin_next ^= 1;
     std::copy(host.begin(), host.end(), dst);
     PMSZ_CUDA(cudaMemcpyAsync(dinst, dst, host.size() * sizeof(Inst<T>), cudaMemcpyHostToDevice, s));
+    return PMSZ_OK;
+}
+
+template <typename T>
+int MultiRun<T>::set_zchunk(int zc) {
+    uint64_t tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        Inst<T> &I = host[i];
+        I.g.zc = zc;
+        tpre[i] = static_cast<uint32_t>(tiles);
+        tiles += static_cast<uint64_t>(I.tiles_x) * I.tiles_y * static_cast<uint64_t>((I.g.nz + zc - 1) / zc);
+        if (tiles >= (1ull << 31)) return set_error(PMSZ_ERR_ARG, "batch too large");
+    }
+    tpre[n] = static_cast<uint32_t>(tiles);
+    total_tiles = static_cast<uint32_t>(tiles);
+    PMSZ_CUDA(cudaMemcpyAsync(dtpre, tpre.data(), tpre.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    PMSZ_CUDA(cudaStreamSynchronize(s));  // tpre may change again right after
+    return PMSZ_OK;
+}
+
+template <typename T>
+int MultiRun<T>::tune_zchunk() {
+    int m = 0;
+    const int *cands = zchunk_candidates(&m);
+    int maxnz = 1;
+    for (const Inst<T> &I : host) maxnz = std::max(maxnz, I.g.nz);
+    EventTimer et;
+    int rc = et.init();
+    if (rc) return rc;
+    for (Inst<T> &I : host) {
+        I.active = 1;
+        I.first = 1;
+        I.k = 0;
+    }
+    int best = cands[0];
+    float best_ms = 0.f;
+    for (int c = 0; c < m; ++c) {
+        if ((rc = set_zchunk(cands[c]))) return rc;
+        if ((rc = push_table())) return rc;
+        float t_best = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {  // the first run of each candidate is a warm-up
+            PMSZ_CUDA(cudaMemsetAsync(zero_base, 0, zero_total, s));
+            PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+            k_first_multi<T><<<total_tiles, dim3(kTX, kTY, 1), 0, s>>>(dinst, dtpre, n);
+            PMSZ_CUDA(cudaGetLastError());
+            PMSZ_CUDA(cudaEventRecord(et.ev[1], s));
+            PMSZ_CUDA(cudaEventSynchronize(et.ev[1]));
+            float t = 0.f;
+            PMSZ_CUDA(cudaEventElapsedTime(&t, et.ev[0], et.ev[1]));
+            if (rep > 0 && (t_best == 0.f || t < t_best)) t_best = t;
+        }
+        if (c == 0 || t_best < best_ms) {
+            best_ms = t_best;
+            best = cands[c];
+        }
+        if (cands[c] >= maxnz) break;  // deeper columns are one chunk for every field
+    }
+    record_batch_zchunk(voxels, n, sizeof(T), best);
+    if ((rc = set_zchunk(best))) return rc;
+    PMSZ_CUDA(cudaMemsetAsync(zero_base, 0, zero_total, s));
     return PMSZ_OK;
 }
 
@@ -439,7 +504,8 @@ int batch_impl(const std::vector<FieldSpec<T>> &specs, const pmsz_opts *opts, st
     const int64_t max_sweeps = opts && opts->max_sweeps > 0 ? opts->max_sweeps : 10000;
     if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
     int rc = PMSZ_OK;
-    if (opts && (opts->flags & PMSZ_FLAG_AUTOTUNE))  // the first field of each untuned shape class tunes it
+    const bool tune = opts && (opts->flags & PMSZ_FLAG_AUTOTUNE);
+    if (tune)  // the first field of each untuned shape class tunes it (its single-call parameters)
         for (const FieldSpec<T> &sp : specs)
             if (!tune_known(sp.nx, sp.ny, sp.nz, sizeof(T)) &&
                 (rc = autotune_impl<T>(sp.f, sp.fh, sp.nx, sp.ny, sp.nz, nullptr, s)))
@@ -447,6 +513,7 @@ int batch_impl(const std::vector<FieldSpec<T>> &specs, const pmsz_opts *opts, st
     MultiRun<T> run(s);
     rc = run.setup(specs, max_sweeps, q, s);
     if (rc) return rc;
+    if (tune && !batch_tune_known(run.voxels, run.n, sizeof(T)) && (rc = run.tune_zchunk())) return rc;
     const int n = run.n;
     out.assign(n, BatchOutcome{});
     for (Inst<T> &I : run.host) {

@@ -87,6 +87,12 @@ struct MultiRun {
     // no wait: every generation ends in a read_row, which synchronises the
     // stream before the same copy is written again.
     int push_table();
+    // Sets every field's tile depth (and the tile prefixes) to zc.
+    int set_zchunk(int zc);
+    // Times the first-pass launch over the whole table at each candidate
+    // depth (scratch re-zeroed afterwards), records the fastest for the
+    // batch's size class and sets it.
+    int tune_zchunk();
 
     cudaStream_t s;
     Workspace ws;
@@ -103,7 +109,10 @@ struct MultiRun {
     MultiLists ml;
     bool lists = false;
     Inst<T> *pin = nullptr;  // 2 * n table entries, pinned
-    int pin_next = 0;  // voxel-list generations (all fields together below 2^32 voxels)
+    int pin_next = 0;
+    unsigned char *zero_base = nullptr;  // the scratch that starts zeroed (counters, bitmaps, slots)
+    size_t zero_total = 0;
+    size_t voxels = 0;  // voxel-list generations (all fields together below 2^32 voxels)
 };
 
 // One generation over a device table of n fields (see MultiRun::generation),

@@ -117,6 +117,12 @@ int labels_impl(const uint8_t *codes, size_t nx, size_t ny, size_t nz, uint32_t 
 int tuned_zchunk(size_t nx, size_t ny, size_t nz, size_t elem);
 int tuned_jump_rounds(size_t nx, size_t ny, size_t nz);
 bool tune_known(size_t nx, size_t ny, size_t nz, size_t elem);
+// The batch tile depth of a batch's size class (voxels, field count, element
+// size), tuned over the whole table; and the candidate depths.
+int tuned_batch_zchunk(size_t voxels, int nfields, size_t elem);
+bool batch_tune_known(size_t voxels, int nfields, size_t elem);
+void record_batch_zchunk(size_t voxels, int nfields, size_t elem, int zc);
+const int *zchunk_candidates(int *count);
 template <typename T>
 int autotune_impl(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, pmsz_tune *out, cudaStream_t s);
 // The tuner's measurements: the fused first pass at each tile depth

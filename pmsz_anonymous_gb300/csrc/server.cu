@@ -17,6 +17,7 @@
 // alone through pmsz_correct_*.
 #include "batch.h"
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -260,8 +261,19 @@ private:
             geoms[i] = G.host[i].g;
             voxels += geoms[i].n;
         }
+        // Voxel-list generations pay off once the running set's next active
+        // sets are large (estimate: 15 * changed + fdir of the last sweep, a
+        // sixteenth of a joining field); small groups take the two round-based
+        // launches, which cost less than the list form's eight.
+        unsigned long long est = 0;
+        for (int i = 0; i < n; ++i) {
+            const Job &j = *G.jobs[i];
+            if (j.first || j.log.empty()) est += j.g.n / 16;
+            else est += 15ull * j.log.back().changed + j.log.back().fdir;
+        }
         std::vector<uint32_t> wpre;
-        const bool lists = list_prefixes(geoms, wpre, G.ml.total_words);
+        const bool lists = est >= std::max<unsigned long long>(1ull << 20, voxels / 32) &&
+                           list_prefixes(geoms, wpre, G.ml.total_words);
         if (lists) {
             if ((rc = ensure_lists(G, voxels))) return rc;
             G.ml.wpre = G.dwpre;

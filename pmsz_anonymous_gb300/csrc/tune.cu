@@ -8,16 +8,22 @@
 //   jump_rounds  three-hop pointer jumps per vertex per launch of the label
 //                passes (more rounds, fewer launches and host flag reads).
 // A shape class is (ceil log2 nx, ceil log2 ny, ceil log2 nz) and, for the
-// tile depth, the element size.  autotune_impl times every candidate on the
-// caller's device fields (first pass on f / fhat; AS labels of f's codes)
-// and records the fastest; every entry point reads the table (make_geom's
-// default depth and one round per launch when a class has no entry).  The
-// table is process-wide behind a mutex and persists as text:
-//   "pmsz-tune 1" header, then per entry
-//   "<elem> <bx> <by> <bz> <zchunk> <jump_rounds>".
+// tile depth, the element size.  A batch (pmsz_correct_batch) runs its first
+// pass as one launch over all its fields, so it has a tile depth of its own,
+// tuned on the whole table (batch.cu) and keyed by its size class: ceil log2
+// of its voxels, ceil log2 of its field count, and the element size.
+// autotune_impl times every candidate on the caller's device fields (first
+// pass on f / fhat; AS labels of f's codes) and records the fastest; every
+// entry point reads the table (make_geom's default depth and one round per
+// launch when a class has no entry).  The table is process-wide behind a
+// mutex and persists as text:
+//   "pmsz-tune 1" header, then per field entry
+//   "<elem> <bx> <by> <bz> <zchunk> <jump_rounds>" and per batch entry
+//   "b <elem> <bvoxels> <bfields> <zchunk>".
 #include "common.cuh"
 #include "internal.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -45,7 +51,13 @@ struct Table {
     std::mutex mu;
     std::map<uint32_t, int> zc;      // (elem << 18) | shape key -> tile depth
     std::map<uint32_t, int> rounds;  // shape key -> rounds per launch
+    std::map<uint32_t, int> batch;   // (elem << 12) | (voxel class << 6) | field class -> tile depth
 };
+
+uint32_t batch_key(size_t voxels, int nfields, size_t elem) {
+    return (static_cast<uint32_t>(elem) << 12) | (static_cast<uint32_t>(ceil_log2(voxels)) << 6) |
+           static_cast<uint32_t>(ceil_log2(static_cast<size_t>(std::max(nfields, 1))));
+}
 
 Table &table() {
     static Table t;
@@ -74,6 +86,30 @@ bool tune_known(size_t nx, size_t ny, size_t nz, size_t elem) {
     Table &t = table();
     std::lock_guard<std::mutex> lk(t.mu);
     return t.zc.count((static_cast<uint32_t>(elem) << 18) | shape_key(nx, ny, nz)) != 0;
+}
+
+int tuned_batch_zchunk(size_t voxels, int nfields, size_t elem) {
+    Table &t = table();
+    std::lock_guard<std::mutex> lk(t.mu);
+    auto it = t.batch.find(batch_key(voxels, nfields, elem));
+    return it == t.batch.end() ? kZChunkDefault : it->second;
+}
+
+bool batch_tune_known(size_t voxels, int nfields, size_t elem) {
+    Table &t = table();
+    std::lock_guard<std::mutex> lk(t.mu);
+    return t.batch.count(batch_key(voxels, nfields, elem)) != 0;
+}
+
+void record_batch_zchunk(size_t voxels, int nfields, size_t elem, int zc) {
+    Table &t = table();
+    std::lock_guard<std::mutex> lk(t.mu);
+    t.batch[batch_key(voxels, nfields, elem)] = zc;
+}
+
+const int *zchunk_candidates(int *count) {
+    *count = 4;
+    return kZCands;
 }
 
 static void record(size_t nx, size_t ny, size_t nz, size_t elem, int zc, int rounds) {
@@ -175,6 +211,8 @@ extern "C" int pmsz_tune_save(const char *path) {
         std::fprintf(fp, "%u %u %u %u %d %d\n", kv.first >> 18, k & 63u, (k >> 6) & 63u, (k >> 12) & 63u, kv.second,
                      r == t.rounds.end() ? kDefaultRounds : r->second);
     }
+    for (const auto &kv : t.batch)
+        std::fprintf(fp, "b %u %u %u %d\n", kv.first >> 12, (kv.first >> 6) & 63u, kv.first & 63u, kv.second);
     const bool ok = std::fclose(fp) == 0;
     return ok ? PMSZ_OK : set_error(PMSZ_ERR_IO, std::string("write failed: ") + path);
 }
@@ -183,30 +221,52 @@ extern "C" int pmsz_tune_load(const char *path) {
     if (!path) return set_error(PMSZ_ERR_ARG, "null path");
     FILE *fp = std::fopen(path, "r");
     if (!fp) return set_error(PMSZ_ERR_IO, std::string("cannot open ") + path);
+    char line[256];
     int version = 0;
-    if (std::fscanf(fp, "pmsz-tune %d", &version) != 1 || version != 1) {
+    if (!std::fgets(line, sizeof line, fp) || std::sscanf(line, "pmsz-tune %d", &version) != 1 || version != 1) {
         std::fclose(fp);
         return set_error(PMSZ_ERR_IO, std::string("not a tuning table: ") + path);
     }
-    std::map<uint32_t, int> zc, rounds;
-    unsigned e, bx, by, bz;
-    int z, r, got;
-    while ((got = std::fscanf(fp, "%u %u %u %u %d %d", &e, &bx, &by, &bz, &z, &r)) == 6) {
-        if (!valid_elem(e) || bx > 63 || by > 63 || bz > 63 || z < 1 || z > 256 || r < 1 || r > 16) {
-            std::fclose(fp);
-            return set_error(PMSZ_ERR_IO, std::string("bad tuning entry in ") + path);
+    std::map<uint32_t, int> zc, rounds, batch;
+    bool ok = true;
+    while (ok && std::fgets(line, sizeof line, fp)) {
+        unsigned e, a1, a2, a3;
+        int z, r;
+        char tail;
+        if (line[0] == '\n' || line[0] == '\0') continue;
+        if (line[0] == 'b') {
+            ok = std::sscanf(line, "b %u %u %u %d %c", &e, &a1, &a2, &z, &tail) == 4 && valid_elem(e) && a1 <= 63 &&
+                 a2 <= 63 && z >= 1 && z <= 256;
+            if (ok) batch[(e << 12) | (a1 << 6) | a2] = z;
+        } else {
+            ok = std::sscanf(line, "%u %u %u %u %d %d %c", &e, &a1, &a2, &a3, &z, &r, &tail) == 6 && valid_elem(e) &&
+                 a1 <= 63 && a2 <= 63 && a3 <= 63 && z >= 1 && z <= 256 && r >= 1 && r <= 16;
+            if (ok) {
+                const uint32_t k = a1 | (a2 << 6) | (a3 << 12);
+                zc[(e << 18) | k] = z;
+                rounds[k] = r;
+            }
         }
-        const uint32_t k = bx | (by << 6) | (bz << 12);
-        zc[(e << 18) | k] = z;
-        rounds[k] = r;
     }
     std::fclose(fp);
-    if (got != EOF) return set_error(PMSZ_ERR_IO, std::string("malformed tuning table: ") + path);
+    if (!ok) return set_error(PMSZ_ERR_IO, std::string("bad tuning entry in ") + path);
     Table &t = table();
     std::lock_guard<std::mutex> lk(t.mu);
     for (const auto &kv : zc) t.zc[kv.first] = kv.second;
     for (const auto &kv : rounds) t.rounds[kv.first] = kv.second;
+    for (const auto &kv : batch) t.batch[kv.first] = kv.second;
     return PMSZ_OK;
+}
+
+extern "C" int pmsz_tune_batch_get(size_t total_voxels, int count, size_t elem_size, pmsz_tune *out) {
+    if (!out || !valid_elem(elem_size) || total_voxels == 0 || count < 1) {
+        set_error(PMSZ_ERR_ARG, "bad arguments to pmsz_tune_batch_get");
+        return -PMSZ_ERR_ARG;
+    }
+    *out = pmsz_tune{};
+    out->zchunk = tuned_batch_zchunk(total_voxels, count, elem_size);
+    out->jump_rounds = kDefaultRounds;
+    return batch_tune_known(total_voxels, count, elem_size) ? 1 : 0;
 }
 
 extern "C" void pmsz_tune_clear(void) {
@@ -214,4 +274,5 @@ extern "C" void pmsz_tune_clear(void) {
     std::lock_guard<std::mutex> lk(t.mu);
     t.zc.clear();
     t.rounds.clear();
+    t.batch.clear();
 }

@@ -107,8 +107,32 @@ def test_batch_with_autotune_matches_oracle(cuda):
         f, fh = _case(shape, dtype, comp, eb, seed)
         refs.append(O.correct(f, fh, eb)[0])
         items.append((_dev(f, cuda), _dev(fh, cuda), eb))
+    total = sum(int(np.prod(c[0])) for c in cases)
+    assert api().tune_batch_get(total, len(cases), torch.float32) == (False, 32)
     res = api().correct_batch(items, autotune=True)
+    known, zc = api().tune_batch_get(total, len(cases), torch.float32)
+    assert known and zc in (8, 16, 32, 64)
     for (shape, *_), (_, dfh, _), ref, r in zip(cases, items, refs, res):
         assert r.status == 0
         assert api().tune_get(shape, torch.float32)[0] is True
+        np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+
+
+@pytest.mark.parametrize("zchunk", [8, 64])
+def test_batch_results_do_not_depend_on_batch_tile_depth(cuda, tmp_path, zchunk):
+    cases = [((40, 33, 70), np.float32, "sz3", 2e-3, 41), ((20, 64, 20), np.float32, "zfp", 1e-3, 42)]
+    total = sum(int(np.prod(c[0])) for c in cases)
+    # a recorded batch depth (through the text table) is what the batch runs at
+    p = tmp_path / "t.txt"
+    p.write_text("pmsz-tune 1\nb 4 %d %d %d\n" % ((total - 1).bit_length(), 1, zchunk))
+    api().tune_load(str(p))
+    assert api().tune_batch_get(total, 2, torch.float32) == (True, zchunk)
+    items, refs = [], []
+    for shape, dtype, comp, eb, seed in cases:
+        f, fh = _case(shape, dtype, comp, eb, seed)
+        refs.append(O.correct(f, fh, eb)[0])
+        items.append((_dev(f, cuda), _dev(fh, cuda), eb))
+    for r in api().correct_batch(items):
+        assert r.status == 0
+    for (_, dfh, _), ref in zip(items, refs):
         np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))

@@ -128,6 +128,24 @@ def test_tuning_table_round_trip_without_gpu(lib, tmp_path):
         lib.pmsz_tune_clear()
 
 
+def test_batch_tuning_entries_load_and_save(lib, tmp_path):
+    lib.pmsz_tune_clear()
+    try:
+        t = capi.Tune()
+        assert lib.pmsz_tune_batch_get(200_000_000, 64, 4, ctypes.byref(t)) == 0 and t.zchunk == 32
+        p = tmp_path / "b.txt"
+        p.write_text("pmsz-tune 1\nb 4 28 6 16\n4 5 5 5 8 2\n")
+        assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_OK
+        assert lib.pmsz_tune_batch_get(200_000_000, 64, 4, ctypes.byref(t)) == 1 and t.zchunk == 16
+        assert lib.pmsz_tune_batch_get(200_000_000, 64, 8, ctypes.byref(t)) == 0  # per element size
+        q = tmp_path / "c.txt"
+        assert lib.pmsz_tune_save(str(q).encode()) == capi.PMSZ_OK
+        assert sorted(q.read_text().splitlines()[1:]) == ["4 5 5 5 8 2", "b 4 28 6 16"]
+        assert lib.pmsz_tune_batch_get(0, 64, 4, ctypes.byref(t)) < 0
+    finally:
+        lib.pmsz_tune_clear()
+
+
 def test_tuning_table_rejects_bad_entries(lib, tmp_path):
     bad = [capi.Tune(0, 1), capi.Tune(300, 1), capi.Tune(32, 0), capi.Tune(32, 17)]
     for t in bad:
@@ -136,6 +154,8 @@ def test_tuning_table_rejects_bad_entries(lib, tmp_path):
     assert lib.pmsz_tune_get(8, 8, 8, 3, ctypes.byref(capi.Tune())) < 0
     p = tmp_path / "bad.txt"
     p.write_text("pmsz-tune 1\n4 3 3 3 0 1\n")
+    assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
+    p.write_text("pmsz-tune 1\nb 4 3 3 300\n")
     assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
     p.write_text("something else\n")
     assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
