@@ -122,30 +122,10 @@ struct TileSmem<T, NF, false> {
     uint32_t xn, xbase;
 };
 
-// The tile of a pass: fp32 fields stage their full 32-bit keys in place of
-// proxies (exact decisions at the proxies' cost, never a failed
-// certificate), fp64 fields stage proxies, plus full keys unless the pass
-// defers failed certificates.
+// The tile of a pass: proxies, plus full keys unless the pass defers failed
+// certificates.
 template <typename T, int MODE, bool DEFER>
-using TileOf = TileSmem<T, MODE == kFirst ? 2 : 1, !DEFER && sizeof(T) == 8>;
-
-// Exact steepest ranks of 15 in-domain 32-bit keys: the highest rank among
-// the maxima and the lowest among the minima (arg_ext's tie rule).
-__device__ __forceinline__ void key_ext_interior(const uint32_t (&k)[15], int &asc, int &desc) {
-    uint32_t M = k[0], m = k[0];
-#pragma unroll
-    for (int r = 1; r < 15; ++r) {
-        M = max(M, k[r]);
-        m = min(m, k[r]);
-    }
-    asc = 0;
-    desc = 14;
-#pragma unroll
-    for (int r = 0; r < 15; ++r) {
-        asc = k[r] == M ? r : asc;
-        desc = k[14 - r] == m ? 14 - r : desc;
-    }
-}
+using TileOf = TileSmem<T, MODE == kFirst ? 2 : 1, !DEFER>;
 
 __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; }
 
@@ -176,7 +156,6 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
     static_assert(!DEFER || MODE == kFirst, "only the first pass defers");
     constexpr int NF = MODE == kFirst ? 2 : 1;
     using K = typename KeyOf<T>::type;
-    constexpr bool kExactKey = sizeof(T) == 4;  // fp32: the tile holds full keys
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
     const int x0 = bx * kTX, y0 = by * kTY;
     const int zb = bz * g.zc, ze = min(g.nz, zb + g.zc);
@@ -215,14 +194,14 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
                 if (in) {
                     const T v = (F == 0 ? fa : fb)[zoff + cell_g[j]];
                     key = okey(v);
-                    px = kExactKey ? static_cast<uint32_t>(key) : proxy_of_key(key);
+                    px = proxy_of_key(key);
                     if (MODE == kFirst && cell_own[j] && zown) {
                         bad |= bad_value(v) ? 1u : 0u;
-                        if (F == 1) hp[zoff + cell_g[j]] = proxy_of_key(key);
+                        if (F == 1) hp[zoff + cell_g[j]] = px;
                     }
                 }
                 (&sm.p[F][s][0][0])[cell_s[j]] = px;
-                if constexpr (!DEFER && !kExactKey) (&sm.k[F][s][0][0])[cell_s[j]] = key;
+                if constexpr (!DEFER) (&sm.k[F][s][0][0])[cell_s[j]] = key;
                 (void)key;
             }
         }
@@ -232,15 +211,8 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
         uint32_t t[15];
 #pragma unroll
         for (int r = 0; r < 15; ++r) t[r] = sm.p[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
-        if constexpr (kExactKey) {  // the staged values are the keys
-            Ext e;
-            e.exact = true;
-            if (interior) key_ext_interior(t, e.asc, e.desc);
-            else arg_ext(t, valid_mask(x, y, z, g.nx, g.ny, g.nz), e.asc, e.desc);
-            return e;
-        }
         Ext e = interior ? proxy_ext_interior(t) : proxy_ext(t);
-        if constexpr (!DEFER && !kExactKey) {
+        if constexpr (!DEFER) {
             if (!e.exact) {  // ties in the truncated proxies: exact keys
                 K k[15];
 #pragma unroll
