@@ -100,7 +100,13 @@ __device__ __forceinline__ Ext proxy_ext_interior(const uint32_t (&t)[15]) {
     return e;
 }
 
-constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2, kRing = 4;
+constexpr int kTX = 32, kTY = 8, kHX = kTX + 2, kHY = kTY + 2;
+// Planes in the shared-memory ring: 4, one plane computed per barrier; the
+// proxy-only tile of the deferring fp32 first pass keeps 8 and computes two
+// planes per barrier (fp64 at two planes spills at its 40-register budget and
+// measured slower).
+template <typename T, bool KEYS>
+constexpr int kRingOf = (KEYS || sizeof(T) == 8) ? 4 : 8;
 constexpr int kCells = kHX * kHY, kThreads = kTX * kTY;
 enum TileMode { kFirst = 0, kDetect = 1, kCodes = 2 };
 
@@ -112,12 +118,12 @@ template <typename T, int NF, bool KEYS>
 struct TileSmem;
 template <typename T, int NF>
 struct TileSmem<T, NF, true> {
-    uint32_t p[NF][kRing][kHY][kHX];                  // proxies
-    typename KeyOf<T>::type k[NF][kRing][kHY][kHX];   // full keys, for the rare exact path
+    uint32_t p[NF][kRingOf<T, true>][kHY][kHX];                  // proxies
+    typename KeyOf<T>::type k[NF][kRingOf<T, true>][kHY][kHX];   // full keys, for the rare exact path
 };
 template <typename T, int NF>
 struct TileSmem<T, NF, false> {
-    uint32_t p[NF][kRing][kHY][kHX];  // proxies
+    uint32_t p[NF][kRingOf<T, false>][kHY][kHX];  // proxies
     uint32_t x[kFirstXCap];           // voxels whose certificate failed
     uint32_t xn, xbase;
 };
@@ -132,8 +138,9 @@ __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; 
 // ---------------------------------------------------------------------------
 // Tiled full-field pass.  Block (32, 8) owns a 32x8 column of the field and
 // marches it through g.zc planes; planes (with a one-voxel halo) stream
-// through a 4-slot ring in shared memory, prefetched two planes ahead, one
-// barrier per plane.  Each thread loads the same (at most two) cells of every
+// through a ring in shared memory (4 slots, one plane computed per barrier;
+// 8 slots and two planes per barrier for the proxy-only deferring fp32 pass),
+// prefetched ahead of the planes being computed.  Each thread loads the same (at most two) cells of every
 // plane, so their coordinates are decoded once per block.
 //   kFirst : fa = f, fb = fhat.  Labels f (code byte), writes the proxy array
 //            of fhat, and runs the first detection (iscriticle data_type=1
@@ -155,6 +162,8 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
                                            uint32_t *xcount = nullptr) {
     static_assert(!DEFER || MODE == kFirst, "only the first pass defers");
     constexpr int NF = MODE == kFirst ? 2 : 1;
+    constexpr int kRing = kRingOf<T, !DEFER>;
+    constexpr int kPer = kRing / 4;  // planes computed per barrier
     using K = typename KeyOf<T>::type;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
     const int x0 = bx * kTX, y0 = by * kTY;
@@ -228,58 +237,66 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
         if (threadIdx.x == 0 && threadIdx.y == 0) sm.xn = 0;  // made visible by the prologue barrier
     }
 
-    load_plane(zb - 1);
-    load_plane(zb);
-    if (zb + 1 <= ze) load_plane(zb + 1);
+    // planes zb-1 .. zb+kPer (those up to ze) before the loop; each iteration
+    // prefetches the kPer planes after the ones it reads, into ring slots last
+    // read kPer iterations earlier (a barrier ends every iteration)
+#pragma unroll
+    for (int zz = zb - 1; zz <= zb + kPer; ++zz)
+        if (zz <= ze) load_plane(zz);
     __syncthreads();
     uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
     const bool in = x < g.nx && y < g.ny;
     const bool xy_interior = x0 >= 1 && x0 + kTX <= g.nx - 1 && y >= 1 && y <= g.ny - 2;  // warp-uniform
-    for (int z = zb; z < ze; ++z) {
-        if (z + 2 <= ze) load_plane(z + 2);
-        const int slots[3] = {(z + kRing - 1) & (kRing - 1), z & (kRing - 1), (z + 1) & (kRing - 1)};
-        const bool interior = xy_interior && z >= 1 && z <= g.nz - 2;
-        uint32_t tm = 0;
-        if (in) {
-            const size_t i = flat(g, x, y, z);
-            if (MODE == kCodes) {
-                const Ext e = ext(0, z, slots, interior);
-                codes[i] = static_cast<uint8_t>(e.asc | (e.desc << 4));
-            } else {
-                int oasc, odesc;
-                Ext e;
-                bool decided = true;
-                if (MODE == kFirst) {
-                    const Ext o = ext(0, z, slots, interior);
-                    oasc = o.asc;
-                    odesc = o.desc;
-                    e = ext(1, z, slots, interior);
-                    if (DEFER && !(o.exact && e.exact)) {
-                        decided = false;
-                        if constexpr (DEFER) {
-                            const uint32_t pos = atomicAdd(&sm.xn, 1u);
-                            if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
-                            else xlist[atomicAdd(xcount, 1u)] = static_cast<uint32_t>(i);
+    for (int z0 = zb; z0 < ze; z0 += kPer) {
+#pragma unroll
+        for (int p = 1; p <= kPer; ++p)
+            if (z0 + kPer + p <= ze) load_plane(z0 + kPer + p);
+#pragma unroll 1
+        for (int z = z0; z < min(z0 + kPer, ze); ++z) {
+            const int slots[3] = {(z + kRing - 1) & (kRing - 1), z & (kRing - 1), (z + 1) & (kRing - 1)};
+            const bool interior = xy_interior && z >= 1 && z <= g.nz - 2;
+            uint32_t tm = 0;
+            if (in) {
+                const size_t i = flat(g, x, y, z);
+                if (MODE == kCodes) {
+                    const Ext e = ext(0, z, slots, interior);
+                    codes[i] = static_cast<uint8_t>(e.asc | (e.desc << 4));
+                } else {
+                    int oasc, odesc;
+                    Ext e;
+                    bool decided = true;
+                    if (MODE == kFirst) {
+                        const Ext o = ext(0, z, slots, interior);
+                        oasc = o.asc;
+                        odesc = o.desc;
+                        e = ext(1, z, slots, interior);
+                        if (DEFER && !(o.exact && e.exact)) {
+                            decided = false;
+                            if constexpr (DEFER) {
+                                const uint32_t pos = atomicAdd(&sm.xn, 1u);
+                                if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
+                                else xlist[atomicAdd(xcount, 1u)] = static_cast<uint32_t>(i);
+                            }
+                        } else {
+                            codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
                         }
                     } else {
-                        codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
+                        const uint8_t c = codes[i];
+                        oasc = c & 15;
+                        odesc = c >> 4;
+                        e = ext(0, z, slots, interior);
                     }
-                } else {
-                    const uint8_t c = codes[i];
-                    oasc = c & 15;
-                    odesc = c >> 4;
-                    e = ext(0, z, slots, interior);
+                    if (decided) {
+                        tm = detect_rules(e.asc, e.desc, oasc, odesc, cmax, cmin, cdir);
+                        if (tm) request_targets(req, g, x, y, z, tm);
+                    }
+                    ++active;
                 }
-                if (decided) {
-                    tm = detect_rules(e.asc, e.desc, oasc, odesc, cmax, cmin, cdir);
-                    if (tm) request_targets(req, g, x, y, z, tm);
-                }
-                ++active;
             }
-        }
-        if (MODE != kCodes) {
-            const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
-            if (tx == 0 && y < g.ny && mism) act_next[word_of(g, x0, y, z)] = mism;
+            if (MODE != kCodes) {
+                const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
+                if (tx == 0 && y < g.ny && mism) act_next[word_of(g, x0, y, z)] = mism;
+            }
         }
         __syncthreads();
     }
