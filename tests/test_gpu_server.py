@@ -104,3 +104,25 @@ def test_budget_limits_admission_and_rejects_oversized_jobs(cuda):
     for j, info, w in zip(jobs, infos, work):
         _check(j, info, w)
     assert max(i["queue_ms"] for i in infos) >= 0.0
+
+
+def test_large_group_runs_list_generations_and_matches_alone(cuda):
+    # eight 160^3 fields joining together: the running set's estimated active
+    # voxels pass 2^20, so the server takes its voxel-list generations
+    A = _api()
+    jobs = []
+    for k in range(8):
+        comp, eb = ("sz3", 2e-3) if k % 2 else ("zfp", 1e-3)
+        f = A.gen_perlin((160, 160, 160), 500 + k, 4, 1 / 16, dtype=torch.float32, device=cuda)
+        fh = A.standin(f, eb, comp, 500 + k)
+        ref = fh.clone()
+        r = A.correct(f, ref, eb)
+        jobs.append((f, fh, eb, ref, r))
+    work = [j[1].clone() for j in jobs]
+    torch.cuda.synchronize()
+    with A.Server() as srv:
+        ids = [srv.submit(j[0], w, j[2]) for j, w in zip(jobs, work)]
+        infos = [srv.wait(i) for i in ids]
+    torch.cuda.synchronize()
+    for j, info, w in zip(jobs, infos, work):
+        _check(j, info, w)
