@@ -26,54 +26,143 @@ namespace pmsz {
 
 constexpr int kTile = 2048;  // voxels per tile: 256 threads x 8
 
+// Step count of an edited voxel, round((p - c) / delta) as the reference
+// computes it.  fp64 division is slow on this GPU (its FP64 pipe runs two
+// operations per SM per cycle), so a candidate k -- the voxel's edit counter
+// when the correction left it, else rint((p - c) * inv) -- is accepted when
+// one fma shows |p - c - k*delta| <= delta/4: then the correctly rounded
+// quotient lies within k +- 0.25 (plus one rounding), and round() gives k.
+// Anything else takes the division.  fp32 divides directly.
+__device__ __forceinline__ uint8_t edit_steps(double p, double c, double delta, double inv, double quarter, int hint) {
+    const double diff = p - c;
+    const double k = hint >= 0 ? static_cast<double>(hint) : rint(diff * inv);
+    if (fabs(k) < 1048576.0 && fabs(fma(-k, delta, diff)) <= quarter) return static_cast<uint8_t>(k);
+    return static_cast<uint8_t>(round(diff / delta));
+}
+__device__ __forceinline__ uint8_t edit_steps(float p, float c, float delta, float, float, int) {
+    return static_cast<uint8_t>(round((p - c) / delta));
+}
+
+// IEEE equality and order of two values on the integer pipe (NaN equals
+// nothing and orders below nothing; +0 and -0 are equal): the tests every
+// voxel takes stay off the slow fp64 pipe.
+__device__ __forceinline__ uint64_t fp_bits(double v) { return static_cast<uint64_t>(__double_as_longlong(v)); }
+__device__ __forceinline__ uint32_t fp_bits(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ bool fp_nan(uint64_t x) { return (x & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull; }
+__device__ __forceinline__ bool fp_nan(uint32_t x) { return (x & 0x7FFFFFFFu) > 0x7F800000u; }
+template <typename T>
+__device__ __forceinline__ bool fp_eq(T a, T b) {
+    const auto x = fp_bits(a), y = fp_bits(b);
+    using U = decltype(x);
+    const U mag = ~(U(1) << (sizeof(U) * 8 - 1));
+    return !fp_nan(x) && !fp_nan(y) && (x == y || ((x | y) & mag) == 0);
+}
+template <typename T>
+__device__ __forceinline__ bool fp_lt(T a, T b) {
+    const auto x = fp_bits(a), y = fp_bits(b);
+    using U = decltype(x);
+    const U sign = U(1) << (sizeof(U) * 8 - 1);
+    if (fp_nan(x) || fp_nan(y) || ((x | y) & ~sign) == 0) return false;
+    const U kx = (x & sign) ? ~x : (x | sign), ky = (y & sign) ? ~y : (y | sign);  // order-preserving keys
+    return kx < ky;
+}
+
 // cnt (optional): the correction's edit counters; a voxel whose counter is 0
 // was never edited, so cur == prev there and its three values need not be read.
-// Per tile: the clamp flags (one ballot word per 32 voxels), the clamp count
-// and the edit count, combined in shared memory (no global atomics: one
-// counter shared by every warp serialises at L2).
+// Each warp first lists the voxels of its 256 whose value changed (in shared
+// memory), then decides them 32 at a time, so the fp64 work of the decision
+// runs on full warps, about once per 256 voxels instead of once per 32.  Per
+// tile: the clamp flags (one word per 32 voxels, set in shared memory), the
+// clamp count and the edit count, combined in shared memory (no global
+// atomics: one counter shared by every warp serialises at L2).
 template <typename T>
 __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, const T *__restrict__ cur,
                                                  const T *__restrict__ f, const uint8_t *__restrict__ cnt, size_t n,
-                                                 T eps, T delta, int q, uint8_t *__restrict__ deltas,
+                                                 T eps, T delta, T inv, T quarter, int q, uint8_t *__restrict__ deltas,
                                                  uint32_t *__restrict__ flags, uint32_t *__restrict__ tile_count,
                                                  uint32_t *__restrict__ tile_edits) {
     __shared__ uint32_t s_cnt, s_edits;
+    __shared__ uint32_t s_fl[kTile / 32];
+    __shared__ uint16_t s_list[8][kTile / 8];  // per warp: changed voxels, offsets within the tile
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_cnt = s_edits = 0;
+    if (threadIdx.x < kTile / 32) s_fl[threadIdx.x] = 0;
     __syncthreads();
     const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
-    uint32_t clamps = 0, edits = 0;
+    // each thread: 8 consecutive voxels (one 8-byte counter load, one 8-byte
+    // delta store); the values of the touched ones are loaded together
+    const uint32_t off0 = static_cast<uint32_t>(threadIdx.x) * 8;
+    const size_t i0 = base + off0;
+    const bool full = i0 + 8 <= n && (reinterpret_cast<uintptr_t>(deltas + i0) & 7) == 0 &&
+                      (!cnt || (reinterpret_cast<uintptr_t>(cnt + i0) & 7) == 0);
+    uint8_t cv[8];
+    if (full && cnt) {
+        const uint2 u = *reinterpret_cast<const uint2 *>(cnt + i0);
 #pragma unroll
-    for (int j = 0; j < kTile / 256; ++j) {
-        const size_t i = base + static_cast<size_t>(j) * 256 + threadIdx.x;
-        bool cl = false;
-        if (i < n) {
-            uint8_t d = 0;
-            const bool touched = !cnt || cnt[i] != 0;
-            const T c = touched ? cur[i] : T(0), p = touched ? prev[i] : T(0);
-            if (touched && c != p) {
-                edits += c < p;
-                const T cv = f[i] - eps;
-                if (c != cv) {
-                    d = static_cast<uint8_t>(round((p - c) / delta));
-                } else {
-                    d = static_cast<uint8_t>(q);
-                    cl = cv != T(0);
+        for (int j = 0; j < 8; ++j) cv[j] = static_cast<uint8_t>(((j < 4 ? u.x : u.y) >> ((j & 3) * 8)) & 0xFFu);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cv[j] = (i0 + j < n) ? (cnt ? cnt[i0 + j] : uint8_t(1)) : uint8_t(0);
+    }
+    T c8[8], p8[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c8[j] = cv[j] ? cur[i0 + j] : T(0);
+        p8[j] = cv[j] ? prev[i0 + j] : T(0);
+    }
+    uint32_t needm = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (cv[j] && !fp_eq(c8[j], p8[j])) needm |= 1u << j;
+    if (full) {  // unchanged voxels: delta 0; changed ones are written below
+        if (needm != 0xFFu) *reinterpret_cast<uint2 *>(deltas + i0) = make_uint2(0u, 0u);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (i0 + j < n && !((needm >> j) & 1u)) deltas[i0 + j] = 0;
+    }
+    const uint32_t cnt8 = __popc(needm);
+    uint32_t inc = cnt8;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    const uint32_t nt = __shfl_sync(0xFFFFFFFFu, inc, 31);  // warp-uniform
+    uint32_t pos = inc - cnt8;
+    for (uint32_t m = needm; m; m &= m - 1) s_list[w][pos++] = static_cast<uint16_t>(off0 + (__ffs(m) - 1));
+    __syncwarp();
+    uint32_t clamps = 0, edits = 0;
+    for (uint32_t k0 = 0; k0 < nt; k0 += 32) {
+        const uint32_t k = k0 + static_cast<uint32_t>(lane);
+        if (k < nt) {
+            const uint32_t off = s_list[w][k];
+            const size_t i = base + off;
+            const T c = cur[i], p = prev[i];
+            edits += fp_lt(c, p);
+            const T cv = f[i] - eps;
+            uint8_t d;
+            if (!fp_eq(c, cv)) {
+                d = edit_steps(p, c, delta, inv, quarter, cnt ? static_cast<int>(cnt[i]) : -1);
+            } else {
+                d = static_cast<uint8_t>(q);
+                if (!fp_eq(cv, T(0))) {
+                    atomicOr(&s_fl[off >> 5], 1u << (off & 31));
+                    ++clamps;
                 }
             }
             deltas[i] = d;
         }
-        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, cl);
-        if ((threadIdx.x & 31) == 0 && (base + static_cast<size_t>(j) * 256 + (threadIdx.x & ~31u)) < n)
-            flags[(base + static_cast<size_t>(j) * 256 + threadIdx.x) >> 5] = bal;
-        clamps += cl;
     }
     clamps = warp_sum_u32(clamps);
     edits = warp_sum_u32(edits);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         if (clamps) atomicAdd(&s_cnt, clamps);
         if (edits) atomicAdd(&s_edits, edits);
     }
     __syncthreads();
+    if (threadIdx.x < kTile / 32 && base + static_cast<size_t>(threadIdx.x) * 32 < n)
+        flags[(base >> 5) + threadIdx.x] = s_fl[threadIdx.x];
     if (threadIdx.x == 0) {
         tile_count[blockIdx.x] = s_cnt;
         tile_edits[blockIdx.x] = s_edits;
@@ -85,37 +174,50 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
 __global__ void __launch_bounds__(1024) k_scan_tiles(uint32_t *__restrict__ counts,
                                                      const uint32_t *__restrict__ edits, size_t m,
                                                      unsigned long long *total) {
-    __shared__ unsigned long long s_part[1024];
-    __shared__ unsigned long long s_edits[32];
-    const size_t per = (m + 1023) / 1024;
-    const size_t lo = threadIdx.x * per, hi = std::min(m, lo + per);
-    unsigned long long sum = 0, esum = 0;
-#pragma unroll 8
-    for (size_t i = lo; i < hi; ++i) {
-        sum += counts[i];
-        esum += edits[i];
+    // chunks of 1024 entries, one per thread (coalesced): warp scans, then the
+    // warps' totals, then the running offset of the chunks before
+    __shared__ unsigned long long s_warp[32];
+    __shared__ unsigned long long s_run;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_run = 0;
+    unsigned long long esum = 0;
+    for (size_t c0 = 0; c0 < m; c0 += 1024) {
+        const size_t i = c0 + threadIdx.x;
+        const unsigned long long v = i < m ? counts[i] : 0ull;
+        if (i < m) esum += edits[i];
+        unsigned long long inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        __syncthreads();  // s_warp / s_run of the previous chunk are consumed
+        if (lane == 31) s_warp[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            const unsigned long long wv = s_warp[lane];
+            unsigned long long winc = wv;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, winc, o);
+                if (lane >= o) winc += t;
+            }
+            s_warp[lane] = winc - wv;  // exclusive offsets of the warps
+        }
+        __syncthreads();
+        const unsigned long long run = s_run;
+        if (i < m) counts[i] = static_cast<uint32_t>(run + s_warp[warp] + inc - v);  // at most n < 2^32 clamp values
+        __syncthreads();
+        if (threadIdx.x == 1023) s_run = run + s_warp[31] + inc;
     }
-    for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xFFFFFFFFu, esum, o);
-    if ((threadIdx.x & 31) == 0) s_edits[threadIdx.x >> 5] = esum;
-    s_part[threadIdx.x] = sum;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
-        const unsigned long long v = threadIdx.x >= static_cast<unsigned>(o) ? s_part[threadIdx.x - o] : 0ull;
-        __syncthreads();
-        s_part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned long long run = s_part[threadIdx.x] - sum;
-#pragma unroll 8
-    for (size_t i = lo; i < hi; ++i) {
-        const uint32_t c = counts[i];
-        counts[i] = static_cast<uint32_t>(run);  // offsets fit: at most n clamp values, n < 2^32 per call
-        run += c;
-    }
-    if (threadIdx.x == 1023) total[0] = s_part[1023];
+    for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xFFFFFFFFu, esum, o);
+    if (lane == 0) s_warp[warp] = esum;
+    __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long e = 0;
-        for (int w = 0; w < 32; ++w) e += s_edits[w];
+        for (int w = 0; w < 32; ++w) e += s_warp[w];
+        total[0] = s_run;
         total[1] = e;
     }
 }
@@ -166,8 +268,9 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
     unsigned long long *tot = ws.at<unsigned long long>(o_tot);
     const T eps = static_cast<T>(eb);
     const T delta = static_cast<T>(eb / static_cast<double>(q));
-    k_extract<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, cur, f, cnt, n, eps, delta, q, deltas, flags, tc,
-                                                              te);
+    const T inv = static_cast<T>(1.0 / static_cast<double>(delta)), quarter = static_cast<T>(0.25 * static_cast<double>(delta));
+    k_extract<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, cur, f, cnt, n, eps, delta, inv, quarter, q, deltas,
+                                                              flags, tc, te);
     k_scan_tiles<<<1, 1024, 0, s>>>(tc, te, tiles, tot);
     k_scatter_clamps<T><<<static_cast<unsigned>((tiles + 7) / 8), 256, 0, s>>>(cur, flags, tc, n, tiles, clamp);
     PMSZ_CUDA(cudaGetLastError());

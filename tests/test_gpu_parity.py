@@ -227,3 +227,40 @@ def test_large_field_through_the_device_sweep_loop(cuda, dtype, comp):
     rf = api().correct(df, full, eb, full_sweeps=True)
     assert rf.sweeps == sw
     assert torch.equal(full.view(torch.uint8), work.view(torch.uint8))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_extract_edits_all_branches_match_oracle(cuda, dtype):
+    # synthetic (prev, cur) pairs: unchanged, k whole steps below (subtracted
+    # step by step, as the correction does), quotients near half steps (the
+    # exact-division fallback), changes below half a step, clamps f - eps,
+    # and clamps of value 0 (dropped from the list); dense enough that some
+    # warps hold more than 32 changed voxels.  (Values raised other than by a
+    # clamp never come out of the correction: their encoding is not pinned.)
+    eb, q = 1e-3, 5
+    rng = np.random.default_rng(21)
+    shape = (40, 64, 66)
+    n = int(np.prod(shape))
+    f = rng.uniform(0.0, 1.0, n).astype(dtype)
+    prev = (f + rng.uniform(-eb, eb, n)).astype(dtype)
+    eps, delta = dtype(eb), dtype(eb / q)
+    cur = prev.copy()
+    kind = rng.integers(0, 10, n)
+    for k in range(1, 5):
+        sel = kind == k
+        for _ in range(k):
+            cur[sel] = (cur[sel] - delta).astype(dtype)
+    sel = kind == 5
+    cur[sel] = (prev[sel] - delta * dtype(2.5) * (1 + rng.uniform(-1e-6, 1e-6, sel.sum()))).astype(dtype)
+    sel = kind == 6  # changed by less than half a step: step count 0
+    cur[sel] = (prev[sel] - delta * dtype(0.3)).astype(dtype)
+    sel = kind == 7
+    cur[sel] = (f[sel] - eps).astype(dtype)
+    zero = np.flatnonzero(kind == 8)[:50]
+    f[zero] = eps
+    cur[zero] = (f[zero] - eps).astype(dtype)
+    d, cl, ec = api().extract_edits(_dev(prev, cuda), _dev(cur, cuda), _dev(f, cuda), eb, q)
+    rd, rcl, rec = O.extract_edits(prev, cur, f, eb, q)
+    np.testing.assert_array_equal(d.cpu().numpy(), rd)
+    np.testing.assert_array_equal(cl.cpu().numpy().view(np.uint8), rcl.view(np.uint8))
+    assert ec == rec
