@@ -298,13 +298,14 @@ def run_ours(args):
     # host output -- the delta symbols and the clamp list -- copied back.
     f_h = f.cpu().pin_memory()
     fh_h = fh0.cpu().pin_memory()
-    deltas_h = torch.empty(n, dtype=torch.uint8).pin_memory()
+    deltas_h = torch.empty(api.packed_len(n), dtype=torch.uint8).pin_memory()
     clamp_h = torch.empty(n, dtype=f.dtype).pin_memory()
     e2e_times, n_clamp, e2e_res = [], 0, None
     for i in range(1 + args.e2e_steps if args.e2e_steps > 0 else 0):
         barrier()
         start.record()
-        e2e_res, extra = api.correct_host(f_h, fh_h, args.eb, deltas=deltas_h, clamp=clamp_h, edits_only=True)
+        e2e_res, extra = api.correct_host(f_h, fh_h, args.eb, deltas=deltas_h, clamp=clamp_h, edits_only=True,
+                                          packed_deltas=True)
         stop.record()
         stop.synchronize()
         n_clamp = extra["n_clamp"]
@@ -332,9 +333,10 @@ def run_ours(args):
                                          "active_per_sweep": [int(v) for v in last.log[:, 6]],
                                          "requested_per_sweep": [int(v) for v in last.log[:, 3]]}),
         "e2e": {"value": whole_job_rate(n, world, e2e_ms), "unit": "Gvox/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": n + n_clamp * itemsize,
-                "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY: H2D f and fhat, correction, "
-                        "edit extraction, D2H delta symbols (1 B/voxel) and clamp list"},
+                "h2d_bytes_per_step": 2 * n * itemsize, "d2h_bytes_per_step": api.packed_len(n) + n_clamp * itemsize,
+                "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY | PMSZ_FLAG_PACKED_DELTAS: H2D f and fhat, "
+                        "correction, edit extraction, D2H delta symbols packed at 3 bits (the reference's "
+                        "pack_nbits) and the clamp list"},
         "roofline": {"bound": "hbm", "kernel": "k_tiled<T,kFirst,DEFER> + k_first_exact (labelling + first detection)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": bytes_first,

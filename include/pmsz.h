@@ -45,6 +45,13 @@ extern "C" {
 #define PMSZ_FLAG_NAIVE 8u        /* pmsz_correct_host_*: run the naive-MSz
                                      strategy (pmsz_correct_naive_*) instead of
                                      the pMSz loop */
+#define PMSZ_FLAG_PACKED_DELTAS 32u /* pmsz_correct_host_*: outs->deltas receives
+                                     the delta symbols packed on the GPU as
+                                     the reference's pack_nbits does
+                                     (pMSz.cu:2328-2348): LSB-first,
+                                     bits_for_max(q) bits each (3 for q = 5),
+                                     ceil(n * bits / 8) bytes -- what
+                                     pmsz_encode_packed_deltas compresses */
 #define PMSZ_FLAG_AUTOTUNE 16u    /* pmsz_correct_{f32,f64} and
                                      pmsz_correct_batch: a field whose shape
                                      class has no entry in the tuning table is

@@ -22,6 +22,9 @@ extern "C" {
  * zstd level 5 (pMSz.cu:2480).
  */
 int pmsz_encode_deltas(const uint8_t *deltas, size_t n, int q, uint8_t **out, size_t *out_len);
+/* The same payload from symbols already packed (PMSZ_FLAG_PACKED_DELTAS):
+ * zstd level 5 of the `len` packed bytes; identical output. */
+int pmsz_encode_packed_deltas(const uint8_t *packed, size_t len, uint8_t **out, size_t *out_len);
 
 /*
  * _edits.bin payload.  Replaces compress_zstd<T> (pMSz.cu:2261-2277, called at
@@ -39,7 +42,9 @@ void pmsz_free(void *p);
 
 /* Optional outputs of pmsz_correct_host_*. */
 typedef struct pmsz_host_outputs {
-    uint8_t *deltas;             /* host array of n bytes: edit symbols, or NULL */
+    uint8_t *deltas;             /* host array of n bytes: edit symbols, or NULL (with
+                                    PMSZ_FLAG_PACKED_DELTAS: ceil(n * bits_for_max(q) / 8)
+                                    bytes of packed symbols) */
     void *clamp;                 /* host array of n values of the field type, or NULL;
                                     the first n_clamp entries are the clamp list */
     uint64_t n_clamp;            /* out */

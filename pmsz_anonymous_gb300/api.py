@@ -99,24 +99,29 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
 
 def correct_host(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
                  deltas: torch.Tensor | None = None, clamp: torch.Tensor | None = None,
-                 edits_only: bool = False, verify: bool = False, device=None, stream=None):
+                 edits_only: bool = False, verify: bool = False, device=None, stream=None,
+                 packed_deltas: bool = False):
     """pmsz_correct_host_*: the single-rank main pipeline on HOST tensors (pin
     them for full copy bandwidth).  fhat is replaced by the corrected field
     unless edits_only.  deltas (uint8, n) and clamp (field dtype, n) receive
-    the edit output when given.  Returns (CorrectResult, dict with n_clamp,
-    edit_count and, with verify, the verification counts)."""
+    the edit output when given; with packed_deltas, deltas receives the
+    symbols packed as the reference's pack_nbits does (packed_len(n, q)
+    bytes, PMSZ_FLAG_PACKED_DELTAS).  Returns (CorrectResult, dict with
+    n_clamp, edit_count and, with verify, the verification counts)."""
     for t, name in ((f, "f"), (fhat, "fhat")):
         if t.device.type != "cpu" or not t.is_contiguous() or t.dtype not in (torch.float32, torch.float64):
             raise ValueError(f"{name} must be a contiguous float32/float64 host tensor")
     if f.shape != fhat.shape or f.dtype != fhat.dtype or f.dim() != 3:
         raise ValueError("f and fhat must be 3-D host tensors of one shape and dtype")
     n = f.numel()
-    if deltas is not None and (deltas.dtype != torch.uint8 or deltas.numel() < n or deltas.device.type != "cpu"):
-        raise ValueError("deltas must be a host uint8 tensor of n entries")
+    dn = packed_len(n, q) if packed_deltas else n
+    if deltas is not None and (deltas.dtype != torch.uint8 or deltas.numel() < dn or deltas.device.type != "cpu"):
+        raise ValueError(f"deltas must be a host uint8 tensor of {dn} entries")
     if clamp is not None and (clamp.dtype != f.dtype or clamp.numel() < n or clamp.device.type != "cpu"):
         raise ValueError("clamp must be a host tensor of the field dtype with n entries")
     L = capi.load()
-    flags = capi.PMSZ_FLAG_EDITS_ONLY if edits_only else 0
+    flags = ((capi.PMSZ_FLAG_EDITS_ONLY if edits_only else 0) |
+             (capi.PMSZ_FLAG_PACKED_DELTAS if packed_deltas else 0))
     opts = capi.Opts(int(q), flags, int(max_sweeps))
     log = (capi.SweepRecord * int(max_sweeps))()
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
@@ -244,6 +249,25 @@ def encode_deltas(deltas: np.ndarray, q: int = 5) -> bytes:
     out, n = ctypes.c_void_p(), ctypes.c_size_t()
     capi.check(L.pmsz_encode_deltas(d.ctypes.data, d.size, int(q), ctypes.byref(out), ctypes.byref(n)))
     return _take(L, out, n.value)
+
+
+def symbol_bits(q: int = 5) -> int:
+    """bits_for_max(q) (pMSz.cu:2352-2356): ceil(log2(q + 1)) bits per delta symbol."""
+    return max(1, int(q).bit_length())
+
+
+def packed_len(n: int, q: int = 5) -> int:
+    """Bytes of n delta symbols packed at symbol_bits(q) bits each."""
+    return (int(n) * symbol_bits(q) + 7) // 8
+
+
+def encode_packed_deltas(packed) -> bytes:
+    """_deltas.bin payload from already packed symbols (pmsz_encode_packed_deltas)."""
+    a = np.ascontiguousarray(np.asarray(packed, dtype=np.uint8))
+    L = capi.load()
+    out, ln = ctypes.c_void_p(), ctypes.c_size_t()
+    capi.check(L.pmsz_encode_packed_deltas(a.ctypes.data, a.size, ctypes.byref(out), ctypes.byref(ln)))
+    return _take(L, out, ln.value)
 
 
 def encode_clamps(values: np.ndarray) -> bytes:

@@ -21,6 +21,7 @@ PMSZ_FLAG_TIMING = 2
 PMSZ_FLAG_EDITS_ONLY = 4
 PMSZ_FLAG_NAIVE = 8
 PMSZ_FLAG_AUTOTUNE = 16
+PMSZ_FLAG_PACKED_DELTAS = 32
 
 
 class Opts(ctypes.Structure):
@@ -91,6 +92,7 @@ SIGNATURES = {
     "pmsz_last_error": (ctypes.c_char_p, []),
     "pmsz_version": (c_int, []),
     "pmsz_encode_deltas": (c_int, [_P, c_size, c_int, _P, _P]),
+    "pmsz_encode_packed_deltas": (c_int, [_P, c_size, _P, _P]),
     "pmsz_encode_clamps": (c_int, [_P, c_size, c_size, _P, _P]),
     "pmsz_decode_deltas": (c_int, [_P, c_size, c_size, c_int, _P]),
     "pmsz_decode_clamps": (c_int, [_P, c_size, c_size, _P, _P]),

@@ -188,14 +188,19 @@ int run(const Args &a) {
     cudaFree(dfh);
 
     std::vector<T> corrected(fh);
-    std::vector<uint8_t> deltas(n);
+    // delta symbols come back packed (bits_for_max(q) bits each), as the
+    // reference's encoder packs them before zstd
+    int nbits = 1;
+    while ((1 << nbits) < a.q + 1 && nbits < 8) ++nbits;
+    std::vector<uint8_t> deltas((n * static_cast<size_t>(nbits) + 7) / 8);
     std::vector<T> clamp(n);
     pmsz_verify_result vr{};
     pmsz_host_outputs outs{};
     outs.deltas = deltas.data();
     outs.clamp = clamp.data();
     outs.verify = a.verify ? &vr : nullptr;
-    pmsz_opts opts{a.q, (a.full ? PMSZ_FLAG_FULL_SWEEPS : 0u) | (a.naive ? PMSZ_FLAG_NAIVE : 0u), a.max_sweeps};
+    pmsz_opts opts{a.q, (a.full ? PMSZ_FLAG_FULL_SWEEPS : 0u) | (a.naive ? PMSZ_FLAG_NAIVE : 0u) | PMSZ_FLAG_PACKED_DELTAS,
+                   a.max_sweeps};
     pmsz_result res{};
     std::cout << "topology preserving started!" << std::endl;
     const auto t0 = std::chrono::steady_clock::now();
@@ -215,7 +220,7 @@ int run(const Args &a) {
 
     uint8_t *cd = nullptr, *ce = nullptr;
     size_t nd = 0, ne = 0;
-    if (pmsz_encode_deltas(deltas.data(), n, a.q, &cd, &nd) || pmsz_encode_clamps(clamp.data(), outs.n_clamp, sizeof(T), &ce, &ne)) {
+    if (pmsz_encode_packed_deltas(deltas.data(), deltas.size(), &cd, &nd) || pmsz_encode_clamps(clamp.data(), outs.n_clamp, sizeof(T), &ce, &ne)) {
         std::fprintf(stderr, "error: edit encoding failed: %s\n", pmsz_last_error());
         return 1;
     }

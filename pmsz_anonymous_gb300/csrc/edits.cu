@@ -283,6 +283,36 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
     return ws.release();
 }
 
+// Thread t packs symbols 8t .. 8t+7 (8 * nbits bits = nbits whole bytes).
+__global__ void __launch_bounds__(256) k_pack_deltas(const uint8_t *__restrict__ deltas, size_t n, int nbits,
+                                                     uint8_t *__restrict__ out, size_t out_len) {
+    const size_t t = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const size_t i0 = t * 8;
+    if (i0 >= n) return;
+    const uint64_t mask = (1ull << nbits) - 1ull;
+    uint64_t v = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (i0 + j < n) v |= (static_cast<uint64_t>(deltas[i0 + j]) & mask) << (j * nbits);
+    const size_t b0 = t * static_cast<size_t>(nbits);
+    for (int b = 0; b < nbits && b0 + b < out_len; ++b) out[b0 + b] = static_cast<uint8_t>(v >> (8 * b));
+}
+
+int bits_for_symbols(int q) {
+    int b = 1;
+    while ((1 << b) < q + 1) ++b;
+    return b;
+}
+
+int pack_deltas_impl(const uint8_t *deltas, size_t n, int nbits, uint8_t *out, cudaStream_t s) {
+    if (nbits < 1 || nbits > 8) return set_error(PMSZ_ERR_ARG, "symbol width must be 1..8 bits");
+    const size_t len = (n * static_cast<size_t>(nbits) + 7) / 8, threads = (n + 7) / 8;
+    if (!threads) return PMSZ_OK;
+    k_pack_deltas<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, s>>>(deltas, n, nbits, out, len);
+    PMSZ_CUDA(cudaGetLastError());
+    return PMSZ_OK;
+}
+
 template int extract_impl<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *, float *,
                                  uint64_t *, uint64_t *, cudaStream_t, const uint8_t *);
 template int extract_impl<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,

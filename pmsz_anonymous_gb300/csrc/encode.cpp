@@ -79,6 +79,11 @@ extern "C" int pmsz_encode_deltas(const uint8_t *deltas, size_t n, int q, uint8_
     return zstd_to_malloc(packed.data(), packed.size(), 5, out, out_len);
 }
 
+extern "C" int pmsz_encode_packed_deltas(const uint8_t *packed, size_t len, uint8_t **out, size_t *out_len) {
+    if ((!packed && len) || !out || !out_len) return pmsz::set_error(PMSZ_ERR_ARG, "bad encoder arguments");
+    return zstd_to_malloc(packed, len, 5, out, out_len);
+}
+
 extern "C" int pmsz_encode_clamps(const void *values, size_t count, size_t elem_size, uint8_t **out,
                                   size_t *out_len) {
     if (!out || !out_len || (count && !values) || (elem_size != 4 && elem_size != 8))

@@ -27,6 +27,10 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     const size_t o_d = ws.reserve<uint8_t>(want_edits ? n : 0);
     const size_t o_c = ws.reserve<T>(want_edits ? n : 0);
     const size_t o_cnt = ws.reserve<uint8_t>(want_edits ? n : 0);
+    const bool packed = opts && (opts->flags & PMSZ_FLAG_PACKED_DELTAS) && outs && outs->deltas;
+    const int nbits = q >= 1 && q <= 255 ? bits_for_symbols(q) : 8;  // q is checked by the correction
+    const size_t plen = packed ? (n * static_cast<size_t>(nbits) + 7) / 8 : 0;
+    const size_t o_pack = ws.reserve<uint8_t>(plen);
     int rc = ws.commit();
     if (rc) return rc;
     T *df = ws.at<T>(o_f), *dfh = ws.at<T>(o_fh), *dprev = ws.at<T>(o_prev), *dclamp = ws.at<T>(o_c);
@@ -52,7 +56,13 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
             return rc;
         outs->n_clamp = nc;
         outs->edit_count = ec;
-        if (outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        if (packed) {  // the reference's pack_nbits on the GPU: n * nbits / 8 bytes cross the host link
+            uint8_t *dp = ws.at<uint8_t>(o_pack);
+            if ((rc = pack_deltas_impl(dd, n, nbits, dp, s))) return rc;
+            PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dp, plen, cudaMemcpyDeviceToHost, s));
+        } else if (outs->deltas) {
+            PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        }
         if (outs->clamp && nc) PMSZ_CUDA(cudaMemcpyAsync(outs->clamp, dclamp, nc * sizeof(T), cudaMemcpyDeviceToHost, s));
     }
     if (want_verify && (rc = verify_impl<T>(df, dfh, nx, ny, nz, eb, outs->verify, s))) return rc;

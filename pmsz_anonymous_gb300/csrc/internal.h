@@ -141,6 +141,11 @@ int codes_impl(const T *v, size_t nx, size_t ny, size_t nz, uint8_t *codes, cuda
 template <typename T>
 int verify_impl(const T *f, const T *fp, size_t nx, size_t ny, size_t nz, double eb, pmsz_verify_result *out,
                 cudaStream_t s);
+// Delta symbols packed LSB-first at nbits bits each (pack_nbits,
+// pMSz.cu:2328-2348) into ceil(n * nbits / 8) bytes; bits_for_max(q) is
+// ceil(log2(q + 1)) (pMSz.cu:2352-2356).
+int bits_for_symbols(int q);
+int pack_deltas_impl(const uint8_t *deltas, size_t n, int nbits, uint8_t *out, cudaStream_t s);
 // cnt (optional): edit counters of the correction that turned prev into cur;
 // voxels with counter 0 are then known unchanged and not read.
 template <typename T>

@@ -59,6 +59,13 @@ def test_host_call_matches_device_call(cuda, case):
         assert extra["edit_count"] == ec_ref
         v = extra["verify"]
         assert v["dir_mismatch"] == 0 and v["ext_mismatch"] == 0 and v["bound_beyond_clamp"] == 0
+    # packed on the GPU: the oracle's pack_nbits of the same symbols, and the
+    # same _deltas.bin payload as packing on the host
+    packed = torch.empty(A.packed_len(n), dtype=torch.uint8).pin_memory()
+    A.correct_host(hf, hfh.clone().pin_memory(), eb, deltas=packed, edits_only=True, packed_deltas=True)
+    sym = d_ref.cpu().numpy()
+    assert packed.numpy().tobytes() == O.pack_nbits(sym, A.symbol_bits(5))
+    assert A.encode_packed_deltas(packed.numpy()) == A.encode_deltas(sym)
 
 
 def test_host_call_with_pageable_buffers_and_naive_flag(cuda):

@@ -161,3 +161,14 @@ def test_tuning_table_rejects_bad_entries(lib, tmp_path):
     assert lib.pmsz_tune_load(str(p).encode()) == capi.PMSZ_ERR_IO
     assert lib.pmsz_tune_load(str(tmp_path / "missing.txt").encode()) == capi.PMSZ_ERR_IO
     assert lib.pmsz_tune_get(8, 8, 8, 4, ctypes.byref(capi.Tune())) == 0  # nothing was recorded
+
+
+def test_packed_delta_encoder_matches_symbol_encoder(lib):
+    from pmsz_anonymous_gb300 import api as A
+    rng = np.random.default_rng(7)
+    for q in (1, 3, 5, 8, 255):
+        sym = rng.integers(0, q + 1, 10_001).astype(np.uint8)
+        nb = A.symbol_bits(q)
+        packed = O.pack_nbits(sym, nb)
+        assert len(packed) == A.packed_len(sym.size, q)
+        assert A.encode_packed_deltas(np.frombuffer(packed, np.uint8)) == A.encode_deltas(sym, q)
