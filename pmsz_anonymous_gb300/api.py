@@ -7,6 +7,7 @@ current torch stream; there is no CPU path.
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -61,6 +62,27 @@ class CorrectResult:
         return self.status == capi.PMSZ_OK
 
 
+_tls = threading.local()
+
+
+def _sweep_log(cap: int):
+    """A per-thread sweep-log buffer of at least `cap` records, reused across
+    calls (the library writes the records of the sweeps it runs)."""
+    buf = getattr(_tls, "log", None)
+    if buf is None or len(buf) < cap:
+        buf = (capi.SweepRecord * int(cap))()
+        _tls.log = buf
+    return buf
+
+
+def _log_rows(log, k: int, first: int = 0) -> np.ndarray:
+    """Records first .. first+k-1 as a (k, 8) uint64 array, columns SWEEP_KEYS."""
+    if k <= 0:
+        return np.zeros((0, len(SWEEP_KEYS)), dtype=np.uint64)
+    w = len(SWEEP_KEYS)
+    return np.frombuffer(log, dtype=np.uint64, count=k * w, offset=first * ctypes.sizeof(capi.SweepRecord)).reshape(k, w).copy()
+
+
 def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
             full_sweeps: bool = False, timing: bool = False, stream=None, strategy: str = "pmsz",
             autotune: bool = False) -> CorrectResult:
@@ -79,7 +101,7 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
     flags = ((capi.PMSZ_FLAG_FULL_SWEEPS if full_sweeps else 0) | (capi.PMSZ_FLAG_TIMING if timing else 0) |
              (capi.PMSZ_FLAG_AUTOTUNE if autotune else 0))
     opts = capi.Opts(int(q), flags, int(max_sweeps))
-    log = (capi.SweepRecord * int(max_sweeps))()
+    log = _sweep_log(int(max_sweeps))
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
     nx, ny, nz = _dims(f)
     with torch.cuda.device(f.device):
@@ -91,8 +113,7 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
             _stream(stream))
     capi.check(st, allow=(capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED))
     n = int(res.sweeps)
-    rows = np.array([[getattr(log[i], k) for k in SWEEP_KEYS] for i in range(n)],
-                    dtype=np.uint64).reshape(n, len(SWEEP_KEYS))
+    rows = _log_rows(log, n)
     return CorrectResult(st, n, int(res.iteration), int(res.edits), rows, float(res.ms_first_pass),
                          float(res.ms_detect), float(res.ms_apply), int(res.launches), float(res.ms_total))
 
@@ -123,7 +144,7 @@ def correct_host(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max
     flags = ((capi.PMSZ_FLAG_EDITS_ONLY if edits_only else 0) |
              (capi.PMSZ_FLAG_PACKED_DELTAS if packed_deltas else 0))
     opts = capi.Opts(int(q), flags, int(max_sweeps))
-    log = (capi.SweepRecord * int(max_sweeps))()
+    log = _sweep_log(int(max_sweeps))
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))
     vres = capi.VerifyResult()
     outs = capi.HostOutputs(deltas.data_ptr() if deltas is not None else None,
@@ -137,8 +158,7 @@ def correct_host(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max
             ctypes.byref(outs), _stream(stream))
     capi.check(st, allow=(capi.PMSZ_OK, capi.PMSZ_ERR_NOT_CONVERGED))
     k = int(res.sweeps)
-    rows = np.array([[getattr(log[i], key) for key in SWEEP_KEYS] for i in range(k)],
-                    dtype=np.uint64).reshape(k, len(SWEEP_KEYS))
+    rows = _log_rows(log, k)
     extra = {"n_clamp": int(outs.n_clamp), "edit_count": int(outs.edit_count)}
     if verify:
         extra["verify"] = {name: int(getattr(vres, name)) for name, _ in capi.VerifyResult._fields_}
@@ -314,7 +334,8 @@ def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None, autot
     items = list(items)
     n = len(items)
     fields = (capi.Field * n)()
-    logs = [(capi.SweepRecord * int(max_sweeps))() for _ in range(n)]
+    logs = _sweep_log(n * int(max_sweeps))  # field k's records start at k * max_sweeps
+    rec = ctypes.sizeof(capi.SweepRecord)
     results = (capi.Result * n)()
     statuses = (ctypes.c_int * n)()
     device = None
@@ -326,7 +347,8 @@ def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None, autot
         device = device or f.device
         nx, ny, nz = _dims(f)
         fields[k] = capi.Field(f.data_ptr(), fh.data_ptr(), nx, ny, nz, float(eb), f.element_size(), 0)
-        results[k].sweep_log = ctypes.cast(logs[k], ctypes.POINTER(capi.SweepRecord))
+        results[k].sweep_log = ctypes.cast(ctypes.addressof(logs) + k * int(max_sweeps) * rec,
+                                           ctypes.POINTER(capi.SweepRecord))
         results[k].sweep_log_cap = int(max_sweeps)
     opts = capi.Opts(int(q), capi.PMSZ_FLAG_AUTOTUNE if autotune else 0, int(max_sweeps))
     with torch.cuda.device(device):
@@ -336,8 +358,7 @@ def correct_batch(items, q: int = 5, max_sweeps: int = 10000, stream=None, autot
     out = []
     for k in range(n):
         m = int(results[k].sweeps)
-        rows = np.array([[getattr(logs[k][i], key) for key in SWEEP_KEYS] for i in range(m)],
-                        dtype=np.uint64).reshape(m, len(SWEEP_KEYS))
+        rows = _log_rows(logs, m, k * int(max_sweeps))
         out.append(CorrectResult(int(statuses[k]), m, int(results[k].iteration), int(results[k].edits), rows))
     return out
 
