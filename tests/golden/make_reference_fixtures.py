@@ -18,7 +18,7 @@ writes one ``.npz`` per case:
                 per-pass counts.
 
 Usage:  python tests/golden/make_reference_fixtures.py [outdir] [--only naive]
-(default outdir gpurun_out/reference_fixtures; the committed copies live in
+(default outdir ./reference_fixtures; the committed copies live in
 tests/golden/).
 """
 from __future__ import annotations
@@ -97,7 +97,7 @@ def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only in args:
         args.remove(only)
-    outdir = args[0] if args else os.path.join(ROOT, "gpurun_out", "reference_fixtures")
+    outdir = args[0] if args else os.path.join(os.getcwd(), "reference_fixtures")
     os.makedirs(outdir, exist_ok=True)
     cubin = build_ref.build_cubin()
     if not cubin:
