@@ -92,3 +92,24 @@ def test_batch_stops_at_max_sweeps_like_alone(cuda, max_sweeps):
             assert b.status == r.status and b.sweeps == r.sweeps <= max_sweeps, k
             np.testing.assert_array_equal(b.log[:, :5], r.log[:, :5], err_msg=f"field {k}")
             assert torch.equal(w.view(torch.uint8), fh.view(torch.uint8)), k
+
+
+def test_dense_active_sets_match_alone(cuda):
+    # sz3 stand-ins at large eps: plateaus make most voxels active after the
+    # first pass, so the batch's compaction takes its dense (word-expanded) form
+    A = _api()
+    specs = [((64, 64, 64), torch.float32, "sz3", 2e-2), ((96, 48, 40), torch.float32, "sz3", 5e-2),
+             ((40, 40, 40), torch.float64, "sz3", 2e-2), ((33, 70, 50), torch.float64, "sz3", 3e-2)]
+    fields = [_make(s, dt, c, eb, 80 + k, cuda) for k, (s, dt, c, eb) in enumerate(specs)]
+    for dtype in (torch.float32, torch.float64):
+        pick = [(fld, spec) for fld, spec in zip(fields, specs) if spec[1] == dtype]
+        alone = []
+        for (f, fh0), spec in pick:
+            fh = fh0.clone()
+            alone.append((fh, A.correct(f, fh, spec[3])))
+        work = [fh0.clone() for (_, fh0), _ in pick]
+        res = A.correct_batch([(f, w, spec[3]) for ((f, _), spec), w in zip(pick, work)])
+        for k, ((fh, r), b, w) in enumerate(zip(alone, res, work)):
+            assert b.status == r.status and b.sweeps == r.sweeps, k
+            np.testing.assert_array_equal(b.log[:, :5], r.log[:, :5], err_msg=f"field {k}")
+            assert torch.equal(w.view(torch.uint8), fh.view(torch.uint8)), k

@@ -264,3 +264,17 @@ def test_extract_edits_all_branches_match_oracle(cuda, dtype):
     np.testing.assert_array_equal(d.cpu().numpy(), rd)
     np.testing.assert_array_equal(cl.cpu().numpy().view(np.uint8), rcl.view(np.uint8))
     assert ec == rec
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_dense_active_sets_match_oracle(cuda, dtype):
+    # most voxels active after the first pass: the voxel-list compaction
+    # expands dense steps word by word
+    eb = 3e-2
+    f, fh = _case((96, 80, 72), dtype, "sz3", eb, 17)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    dfh = _dev(fh, cuda)
+    r = api().correct(_dev(f, cuda), dfh, eb)
+    assert r.status == st and r.sweeps == sw
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
