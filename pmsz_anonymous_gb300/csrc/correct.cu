@@ -428,8 +428,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, s);
         k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, act[1], &ls->cur, g, div_nx, eps,
                                                     delta, q, &ls->go);
+        k_pick_detection<<<1, 32, 0, s>>>(ls, static_cast<unsigned long long>(g.n), list_blocks);
         k_loop_gate<<<1, 32, 0, s>>>(ls, slots, max_sweeps, tail_at, cudaGraphConditionalHandle{}, 0);
-        launches += 4;
+        launches += 5;
         PMSZ_CUDA(cudaGetLastError());
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
 
@@ -459,8 +460,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         for (int half = 0; half < 2; ++half) {
             uint32_t *a_cur = act[half == 0 ? 1 : 0], *a_next = act[half == 0 ? 0 : 1];
             compact_bitmap(a_cur, g, bcnt, list, &ls->lc[0], &ls->go, gg.cs);
-            k_detect_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[0], hp, codes, req, a_next, xlist,
-                                                             &ls->lc[2], &ls->cur, g, div_nx, &ls->go);
+            k_detect_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[0], fh, hp, codes, req, a_next, xlist,
+                                                             &ls->lc[2], &ls->cur, g, div_nx, &ls->go,
+                                                             &ls->exact_keys);
             k_detect_exact<T><<<list_blocks, 256, 0, gg.cs>>>(xlist, &ls->lc[2], fh, codes, req, a_next, &ls->cur, g,
                                                               div_nx, &ls->go);
             compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, gg.cs);

@@ -229,13 +229,19 @@ __device__ __forceinline__ void detect_outcome(const Geom &g, int x, int y, int 
 constexpr uint32_t kExactCap = 2048;  // failed certificates buffered per block
 template <typename T>
 __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restrict__ list, const uint32_t *count,
+                                                     const T *__restrict__ fh,
                                                      const uint32_t *__restrict__ hp, const uint8_t *__restrict__ codes,
                                                      uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
                                                      uint32_t *__restrict__ exact_list, uint32_t *exact_count,
-                                                     SweepSlot *slot, Geom g, FastDiv div_nx, const int *run) {
+                                                     SweepSlot *slot, Geom g, FastDiv div_nx, const int *run,
+                                                     const int *exact_keys) {
     __shared__ uint32_t s_exact[kExactCap];
     __shared__ uint32_t s_n, s_base;
     if (run && *run == 0) return;
+    // fp32 with exact_keys set (k_pick_detection, k_loop_gate): the 4-byte keys
+    // of fhat, gathered as the proxies would be, decide every voxel (no
+    // certificates, nothing deferred)
+    const bool keys = sizeof(T) == 4 && exact_keys && *exact_keys;
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
     const uint32_t m = *count;
@@ -247,6 +253,21 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
         voxel_coords(g, div_nx, i, x, y, z);
         const bool interior = x >= 1 && x <= g.nx - 2 && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
         const uint32_t valid = interior ? kAllValid : valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        const uint8_t c = __ldg(codes + i);
+        ++active;
+        if (keys) {
+            uint32_t kk[15];
+#pragma unroll
+            for (int r = 0; r < 15; ++r) {
+                const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+                kk[r] = ((valid >> r) & 1u) ? static_cast<uint32_t>(okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off))))
+                                            : 0u;
+            }
+            int asc, desc;
+            arg_ext(kk, valid, asc, desc);
+            detect_outcome(g, x, y, z, asc, desc, c, req, act_next, cmax, cmin, cdir);
+            continue;
+        }
         const uint32_t *c0 = hp + i;
         uint32_t t[15];
 #pragma unroll
@@ -254,9 +275,7 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
             const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
             t[r] = ((valid >> r) & 1u) ? __ldg(c0 + off) : 0u;
         }
-        const uint8_t c = __ldg(codes + i);
         const Ext ex = interior ? proxy_ext_interior<true>(t) : proxy_ext<true>(t);
-        ++active;
         if (ex.exact) {
             detect_outcome(g, x, y, z, ex.asc, ex.desc, c, req, act_next, cmax, cmin, cdir);
         } else {  // buffered in shared memory; a full buffer spills straight to the list
@@ -408,10 +427,26 @@ inline void compact_bitmap(uint32_t *bm, const Geom &g, uint32_t *counts, uint32
 struct LoopState {
     long long k;
     int go;
-    int pad;
+    int exact_keys;  // fp32 list detection on exact keys (k_pick_detection)
     uint32_t lc[4];  // active list, request list, exact list
     SweepSlot cur;
 };
+
+// Before the first list sweep (after sweep 0's edits): fp32 fields run the
+// list detection on exact keys when the first pass deferred more than a
+// tenth of the voxels (plateaus of quantised values: each such voxel would
+// be detected twice), or when the first list -- estimated as 15 * changed +
+// fdir of sweep 0 -- would defer, at the first pass's rate, more than half
+// of every detection block's buffer (a list of a billion voxels would
+// otherwise spill its deferrals through one global counter).  k_loop_gate
+// makes the first switch later when a list sweep defers more than a tenth.
+static __global__ void k_pick_detection(LoopState *ls, unsigned long long n, unsigned long long blocks) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const unsigned long long deferred = ls->lc[3];
+    const unsigned long long est = 15ull * ls->cur.changed + ls->cur.fdir;
+    const double spill = static_cast<double>(deferred) * static_cast<double>(est) / static_cast<double>(n);
+    if (10ull * deferred > n || spill > 0.5 * kExactCap * static_cast<double>(blocks)) ls->exact_keys = 1;
+}
 
 // After sweep ls->k: store its counters, decide whether the next sweep runs
 // (not converged, not stuck, no NaN input at sweep 0, sweeps left, and an
@@ -425,6 +460,9 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
         const SweepSlot c = ls->cur;
         const long long k = ls->k;
         slots[k] = c;
+        // a list sweep that deferred more than a tenth of its voxels (failed
+        // certificates) switches the following ones to exact keys, for good
+        if (10ull * ls->lc[2] > ls->lc[0]) ls->exact_keys = 1;
         const bool stop = (k == 0 && c.bad) || (c.fmax == 0 && c.fmin == 0 && c.fdir == 0) || c.progressed == 0 ||
                           k + 1 >= max_sweeps;
         const bool tail = 15ull * c.changed + c.fdir <= tail_at;

@@ -278,3 +278,22 @@ def test_dense_active_sets_match_oracle(cuda, dtype):
     assert r.status == st and r.sweeps == sw
     np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
     np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_plateau_field_matches_oracle(cuda, dtype):
+    # a decompressed copy quantised to steps of 2*eb: over 90 % of its voxels
+    # equal a neighbour, the first pass defers most of them (tied proxies),
+    # and the fp32 list sweeps switch to exact keys; many list sweeps run in
+    # the CUDA-graph loop before the cooperative tail
+    shape, eb = (128, 128, 128), 1e-2
+    f = F.perlin_field(shape, 23, 4, 1 / 32, dtype=dtype)
+    step = dtype(2 * eb)
+    fh = (np.round(f / step) * step).astype(dtype)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    dfh = _dev(fh, cuda)
+    r = api().correct(_dev(f, cuda), dfh, eb)
+    assert r.status == st and r.sweeps == sw
+    assert int(r.log[1, 6]) > (1 << 16)  # sweep 2 runs as a list sweep
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
