@@ -206,6 +206,24 @@ __host__ __device__ __forceinline__ uint32_t row_tail_mask(const Geom &g, int wx
     return rem >= 32 ? 0xFFFFFFFFu : ((1u << rem) - 1u);
 }
 
+// A code byte not yet decided (ranks are 0..14, so no code has a nibble 15).
+constexpr uint8_t kCodeUnset = 0xFF;
+
+// Appends v to a global list with one atomic on the list's counter per group
+// of lanes that reach the call together (each lane's slot is the group's base
+// plus its rank among them).  Used where a full per-block buffer spills:
+// lanes spilling one by one would serialise on that counter.
+__device__ __forceinline__ void spill_append(uint32_t *__restrict__ list, uint32_t *count, uint32_t v) {
+    const uint32_t mask = __activemask();
+    uint32_t lane;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    const uint32_t leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    list[base + __popc(mask & ((1u << lane) - 1u))] = v;
+}
+
 // Per-sweep device counters (one slot per sweep).  fmax/fmin/fdir are the
 // reference's count_f_max / count_f_min / count_f_dir (pMSz.cu:174), counted
 // exactly rather than with the reference's racy `+=`.

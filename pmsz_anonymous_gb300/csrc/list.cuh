@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
         } else {  // buffered in shared memory; a full buffer spills straight to the list
             const uint32_t pos = atomicAdd(&s_n, 1u);
             if (pos < kExactCap) s_exact[pos] = i;
-            else exact_list[atomicAdd(exact_count, 1u)] = i;
+            else spill_append(exact_list, exact_count, i);
         }
     }
     const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, 0u};
@@ -324,7 +324,9 @@ __global__ void __launch_bounds__(256) k_detect_exact(const uint32_t *__restrict
 }
 
 // Voxels the first pass deferred (a failed certificate in f or fhat): the
-// original code byte and the first detection on the full keys of both fields.
+// first detection on the full keys of fhat, and the original code byte on the
+// full keys of f where the first pass left it unset (kCodeUnset: f's own
+// certificate failed).
 template <typename T>
 __global__ void __launch_bounds__(256) k_first_exact(const uint32_t *__restrict__ xlist, const uint32_t *count,
                                                      const T *__restrict__ f, const T *__restrict__ fh,
@@ -341,21 +343,25 @@ __global__ void __launch_bounds__(256) k_first_exact(const uint32_t *__restrict_
         voxel_coords(g, div_nx, i, x, y, z);
         const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
         K kk[15];
-        int oasc, odesc, asc, desc;
+        int asc, desc;
+        uint8_t c = codes[i];
+        if (c == kCodeUnset) {
+            int oasc, odesc;
 #pragma unroll
-        for (int r = 0; r < 15; ++r) {
-            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
-            kk[r] = ((valid >> r) & 1u) ? okey(__ldg(f + (static_cast<ptrdiff_t>(i) + off))) : K(0);
+            for (int r = 0; r < 15; ++r) {
+                const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+                kk[r] = ((valid >> r) & 1u) ? okey(__ldg(f + (static_cast<ptrdiff_t>(i) + off))) : K(0);
+            }
+            arg_ext(kk, valid, oasc, odesc);
+            c = static_cast<uint8_t>(oasc | (odesc << 4));
+            codes[i] = c;
         }
-        arg_ext(kk, valid, oasc, odesc);
 #pragma unroll
         for (int r = 0; r < 15; ++r) {
             const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
             kk[r] = ((valid >> r) & 1u) ? okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off))) : K(0);
         }
         arg_ext(kk, valid, asc, desc);
-        const uint8_t c = static_cast<uint8_t>(oasc | (odesc << 4));
-        codes[i] = c;
         detect_outcome(g, x, y, z, asc, desc, c, req, act_next, cmax, cmin, cdir);
     }
     const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, 0u, 0u};

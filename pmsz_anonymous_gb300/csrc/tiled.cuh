@@ -296,10 +296,13 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
                         e = ext(1, z, slots, interior);
                         if (DEFER && !(o.exact && e.exact)) {
                             decided = false;
+                            // the original's code when its certificate held (only
+                            // fhat's failed, as on plateaus), else the unset mark
+                            codes[i] = o.exact ? static_cast<uint8_t>(oasc | (odesc << 4)) : kCodeUnset;
                             if constexpr (DEFER) {
                                 const uint32_t pos = atomicAdd(&sm.xn, 1u);
                                 if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
-                                else xlist[atomicAdd(xcount, 1u)] = static_cast<uint32_t>(i);
+                                else spill_append(xlist, xcount, static_cast<uint32_t>(i));
                             }
                         } else {
                             codes[i] = static_cast<uint8_t>(oasc | (odesc << 4));
