@@ -306,6 +306,27 @@ int pmsz_extract_edits_f64(const double *prev, const double *cur, const double *
                            uint64_t *n_clamp, uint64_t *edit_count, void *stream);
 
 /*
+ * pmsz_reconstruct_{f32,f64}: the decoder the reference lacks (validateResult,
+ * pMSz.cu:2545-2584, only decompresses); the inverse of pmsz_extract_edits.
+ * Over the n voxels, from the decompressed field prev:
+ *   deltas[i] == q    -> out[i] = the next value of clamp[] (voxel order)
+ *   deltas[i] == k < q -> out[i] = prev[i] lowered k times by delta = (T)(eb/q)
+ *                         in T, the correction's own repeated subtraction
+ *                         (pMSz.cu:631), so out is bit-identical to the
+ *                         corrected field
+ * All arrays are device arrays; out may be prev (in place).  PMSZ_ERR_ARG,
+ * with nothing written, for a symbol above q or a count of q symbols other
+ * than n_clamp (the reference encoder drops clamp values equal to 0, so such
+ * a field cannot be rebuilt from its files).
+ */
+int pmsz_reconstruct_f32(const float *prev, const uint8_t *deltas, const float *clamp,
+                         uint64_t n_clamp, size_t n, double eb, int q, float *out,
+                         void *stream);
+int pmsz_reconstruct_f64(const double *prev, const uint8_t *deltas, const double *clamp,
+                         uint64_t n_clamp, size_t n, double eb, int q, double *out,
+                         void *stream);
+
+/*
  * Synthetic inputs (not part of the reference's path; its generator is
  * generate_perlin.py).  pmsz_gen_perlin_*: normalised Perlin fBm, bit-identical
  * to the numpy generator in pmsz_anonymous_gb300/fields.py.  perm512: host

@@ -226,6 +226,30 @@ def extract_edits(prev: torch.Tensor, cur: torch.Tensor, f: torch.Tensor, eb: fl
     return deltas, clamp[: nc.value], int(ec.value)
 
 
+def reconstruct(prev: torch.Tensor, deltas: torch.Tensor, clamp: torch.Tensor, eb: float, q: int = 5,
+                out: torch.Tensor = None, stream=None) -> torch.Tensor:
+    """The corrected field rebuilt from the decompressed field `prev`, the
+    delta symbols and the clamp list (the inverse of extract_edits; device
+    tensors).  `out` defaults to a new tensor; it may be `prev` itself."""
+    if not isinstance(prev, torch.Tensor) or not prev.is_cuda or not prev.is_contiguous():
+        raise TypeError("prev must be a contiguous CUDA tensor")
+    n = prev.numel()
+    if deltas.dtype != torch.uint8 or deltas.numel() != n or deltas.device != prev.device:
+        raise ValueError("deltas must be a uint8 tensor of prev's size on prev's device")
+    if clamp.dtype != prev.dtype or clamp.device != prev.device:
+        raise ValueError("clamp must have prev's dtype and device")
+    deltas, clamp = deltas.contiguous(), clamp.contiguous()
+    if out is None:
+        out = torch.empty_like(prev)
+    elif out.shape != prev.shape or out.dtype != prev.dtype or out.device != prev.device or not out.is_contiguous():
+        raise ValueError("out must be a contiguous tensor like prev")
+    with torch.cuda.device(prev.device):
+        capi.check(getattr(capi.load(), f"pmsz_reconstruct_{_suffix(prev)}")(
+            prev.data_ptr(), deltas.data_ptr(), clamp.data_ptr() if clamp.numel() else None, clamp.numel(), n,
+            float(eb), int(q), out.data_ptr(), _stream(stream)))
+    return out
+
+
 def gen_perlin(shape, seed: int, octaves: int, base_freq: float, persistence: float = 0.5,
                lacunarity: float = 2.0, dtype=torch.float32, device="cuda", stream=None) -> torch.Tensor:
     """Normalised Perlin fBm on the device (same bits as fields.perlin_field)."""

@@ -84,6 +84,8 @@ SIGNATURES = {
     "pmsz_verify_f64": (c_int, [_P, _P, c_size, c_size, c_size, c_double, _P, _P]),
     "pmsz_extract_edits_f32": (c_int, [_P, _P, _P, c_size, c_double, c_int, _P, _P, _P, _P, _P]),
     "pmsz_extract_edits_f64": (c_int, [_P, _P, _P, c_size, c_double, c_int, _P, _P, _P, _P, _P]),
+    "pmsz_reconstruct_f32": (c_int, [_P, _P, _P, c_u64, c_size, c_double, c_int, _P, _P]),
+    "pmsz_reconstruct_f64": (c_int, [_P, _P, _P, c_u64, c_size, c_double, c_int, _P, _P]),
     "pmsz_gen_perlin_f32": (c_int, [_P, c_size, c_size, c_size, _P, _P, _P, c_int, _P]),
     "pmsz_gen_perlin_f64": (c_int, [_P, c_size, c_size, c_size, _P, _P, _P, c_int, _P]),
     "pmsz_standin_f32": (c_int, [_P, _P, c_size, c_double, c_int, c_u64, _P]),

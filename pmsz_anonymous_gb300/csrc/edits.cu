@@ -313,10 +313,148 @@ int pack_deltas_impl(const uint8_t *deltas, size_t n, int nbits, uint8_t *out, c
     return PMSZ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Reconstruction: the decoder the reference lacks (validateResult,
+// pMSz.cu:2545-2584, only decompresses).  The inverse of the extraction per
+// voxel: delta k < q lowers the decompressed value k times by delta_step in T
+// -- the correction's own repeated subtraction (applyDeltaBuffer_local,
+// pMSz.cu:631), so the result is bit-identical to the corrected field -- and
+// delta q takes the next value of the clamp list (voxel order).  A symbol
+// above q, or a count of q symbols other than the list's length (the
+// reference encoder drops clamp values equal to 0, so such a field cannot be
+// rebuilt from its files), is an argument error found before anything is
+// written.  Kernels: per-tile q flags and counts, the tile scan of the
+// extraction, then every voxel's value.
+// ---------------------------------------------------------------------------
+
+// Per tile: one flag word per 32 voxels (bit set where the symbol is q), the
+// number of q symbols and of symbols above q.  Each thread reads 8 symbols;
+// the four lanes whose symbols share a flag word OR their bytes together.
+__global__ void __launch_bounds__(256) k_recon_flags(const uint8_t *__restrict__ deltas, size_t n, int q,
+                                                     uint32_t *__restrict__ flags, uint32_t *__restrict__ tile_count,
+                                                     uint32_t *__restrict__ tile_bad) {
+    __shared__ uint32_t s_cnt, s_bad;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) s_cnt = s_bad = 0;
+    __syncthreads();
+    const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
+    const size_t i0 = base + static_cast<size_t>(threadIdx.x) * 8;
+    uint32_t qm = 0, bad = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (i0 + j < n) {
+            const int d = deltas[i0 + j];
+            if (d == q) qm |= 1u << j;
+            bad += d > q;
+        }
+    }
+    uint32_t word = qm << ((lane & 3) * 8);
+    word |= __shfl_xor_sync(0xFFFFFFFFu, word, 1);
+    word |= __shfl_xor_sync(0xFFFFFFFFu, word, 2);
+    if ((lane & 3) == 0 && i0 < n) flags[i0 >> 5] = word;
+    const uint32_t cnt = warp_sum_u32(__popc(qm)), nbad = warp_sum_u32(bad);
+    if (lane == 0) {
+        if (cnt) atomicAdd(&s_cnt, cnt);
+        if (nbad) atomicAdd(&s_bad, nbad);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tile_count[blockIdx.x] = s_cnt;
+        tile_bad[blockIdx.x] = s_bad;
+    }
+}
+
+// Every voxel of a tile: its clamp rank is the tile's offset, the q flags of
+// the tile's earlier words (a prefix over the 64 words in shared memory) and
+// the flags below it in its own word.  out may alias prev.
+template <typename T>
+__global__ void __launch_bounds__(256) k_recon_apply(const T *prev, const uint8_t *__restrict__ deltas,
+                                                     const T *__restrict__ clamp, const uint32_t *__restrict__ flags,
+                                                     const uint32_t *__restrict__ tile_off, size_t n, T delta, int q,
+                                                     T *out) {
+    __shared__ uint32_t s_fl[kTile / 32], s_pre[kTile / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
+    const size_t nw = (std::min(n - base, static_cast<size_t>(kTile)) + 31) / 32;
+    if (threadIdx.x < kTile / 32) s_fl[threadIdx.x] = threadIdx.x < nw ? flags[(base >> 5) + threadIdx.x] : 0u;
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive prefix of the popcounts, two words per lane
+        const int lane = threadIdx.x;
+        const uint32_t a = __popc(s_fl[2 * lane]), b = __popc(s_fl[2 * lane + 1]);
+        uint32_t inc = a + b;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        s_pre[2 * lane] = inc - a - b;
+        s_pre[2 * lane + 1] = inc - b;
+    }
+    __syncthreads();
+    const uint32_t t0 = tile_off[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t off = static_cast<uint32_t>(threadIdx.x) * 8 + j;
+        const size_t i = base + off;
+        if (i >= n) break;
+        const int d = deltas[i];
+        T v;
+        if (d == q) {
+            const uint32_t w = off >> 5;
+            v = clamp[t0 + s_pre[w] + __popc(s_fl[w] & ((1u << (off & 31)) - 1u))];
+        } else {
+            v = prev[i];
+            for (int k = 0; k < d; ++k) v = v - delta;
+        }
+        out[i] = v;
+    }
+}
+
+template <typename T>
+int reconstruct_impl(const T *prev, const uint8_t *deltas, const T *clamp, uint64_t n_clamp, size_t n, double eb,
+                     int q, T *out, cudaStream_t s) {
+    if (!prev || !deltas || !out || (n_clamp && !clamp)) return set_error(PMSZ_ERR_ARG, "null pointer");
+    if (n == 0 || n >= (static_cast<size_t>(1) << 32)) return set_error(PMSZ_ERR_ARG, "n must be in 1..2^32-1");
+    if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
+    if (!(eb > 0.0)) return set_error(PMSZ_ERR_ARG, "error bound must be positive");
+    const size_t tiles = (n + kTile - 1) / kTile;
+    Workspace ws(s);
+    const size_t o_flags = ws.reserve<uint32_t>(tiles * (kTile / 32));
+    const size_t o_tiles = ws.reserve<uint32_t>(tiles), o_bad = ws.reserve<uint32_t>(tiles);
+    const size_t o_tot = ws.reserve<unsigned long long>(2);
+    int rc = ws.commit();
+    if (rc) return rc;
+    uint32_t *flags = ws.at<uint32_t>(o_flags), *tc = ws.at<uint32_t>(o_tiles), *tb = ws.at<uint32_t>(o_bad);
+    unsigned long long *tot = ws.at<unsigned long long>(o_tot);
+    k_recon_flags<<<static_cast<unsigned>(tiles), 256, 0, s>>>(deltas, n, q, flags, tc, tb);
+    k_scan_tiles<<<1, 1024, 0, s>>>(tc, tb, tiles, tot);
+    PMSZ_CUDA(cudaGetLastError());
+    unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
+    if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+    PMSZ_CUDA(cudaMemcpyAsync(h, tot, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    PMSZ_CUDA(cudaStreamSynchronize(s));
+    if (h[1]) {
+        ws.release();
+        return set_error(PMSZ_ERR_ARG, std::to_string(h[1]) + " delta symbols above q");
+    }
+    if (h[0] != n_clamp) {
+        ws.release();
+        return set_error(PMSZ_ERR_ARG, "the deltas hold " + std::to_string(h[0]) + " clamp symbols, the clamp list " +
+                                           std::to_string(n_clamp) + " values");
+    }
+    const T delta = static_cast<T>(eb / static_cast<double>(q));
+    k_recon_apply<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, deltas, clamp, flags, tc, n, delta, q, out);
+    PMSZ_CUDA(cudaGetLastError());
+    return ws.release();
+}
+
 template int extract_impl<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *, float *,
                                  uint64_t *, uint64_t *, cudaStream_t, const uint8_t *);
 template int extract_impl<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,
                                   double *, uint64_t *, uint64_t *, cudaStream_t, const uint8_t *);
+template int reconstruct_impl<float>(const float *, const uint8_t *, const float *, uint64_t, size_t, double, int,
+                                     float *, cudaStream_t);
+template int reconstruct_impl<double>(const double *, const uint8_t *, const double *, uint64_t, size_t, double, int,
+                                      double *, cudaStream_t);
 
 }  // namespace pmsz
 
@@ -334,5 +472,17 @@ extern "C" int pmsz_extract_edits_f64(const double *prev, const double *cur, con
                                       uint64_t *edit_count, void *stream) {
     return guarded([&] {
         return extract_impl<double>(prev, cur, f, n, eb, q, deltas, clamp, n_clamp, edit_count, as_stream(stream));
+    });
+}
+extern "C" int pmsz_reconstruct_f32(const float *prev, const uint8_t *deltas, const float *clamp, uint64_t n_clamp,
+                                    size_t n, double eb, int q, float *out, void *stream) {
+    return guarded([&] {
+        return reconstruct_impl<float>(prev, deltas, clamp, n_clamp, n, eb, q, out, as_stream(stream));
+    });
+}
+extern "C" int pmsz_reconstruct_f64(const double *prev, const uint8_t *deltas, const double *clamp, uint64_t n_clamp,
+                                    size_t n, double eb, int q, double *out, void *stream) {
+    return guarded([&] {
+        return reconstruct_impl<double>(prev, deltas, clamp, n_clamp, n, eb, q, out, as_stream(stream));
     });
 }
