@@ -3,6 +3,7 @@
 //
 //   pmsz <path>,<W>,<H>,<D> <eb> <sz3|zfp> <PX> <PY> <PZ> [options]   (pMSz.cu:2625-2667)
 //   pmsz <path> <W> <H> <D> <eb> <sz3|zfp> <PX> <PY> <PZ> [options]    (README.md:68-73)
+//   pmsz --reconstruct <decp>,<W>,<H>,<D> <eb> --out FILE [--deltas F] [--edits F]
 //
 // Reads the raw little-endian field (x fastest, pMSz.cu:274-313), obtains the
 // decompressed copy, runs the correction on the GPU, and writes the
@@ -16,8 +17,14 @@
 // (raw, same type and size), or else from the labelled stand-in of the named
 // compressor (sz3: plateaus, zfp: bounded noise), which is announced on
 // stdout.  Errors print a message and return a non-zero status; nothing aborts.
+//
+// --reconstruct is the decoder the reference lacks (its validateResult,
+// pMSz.cu:2545-2584, only decompresses): from the decompressed field and the
+// _deltas.bin / _edits.bin of a correction it writes the corrected field,
+// bit-identical, through pmsz_reconstruct_*.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -37,11 +44,11 @@
 namespace {
 
 struct Args {
-    std::string path, comp, decp, out;
+    std::string path, comp, decp, out, deltas_file = "_deltas.bin", edits_file = "_edits.bin";
     size_t W = 0, H = 0, D = 0;
     double eb = 0;
     int px = 1, py = 1, pz = 1;
-    bool f32 = false, full = false, verify = false, naive = false;
+    bool f32 = false, full = false, verify = false, naive = false, recon = false;
     int q = 5;
     long long max_sweeps = 10000;
     double cmp_size = 0;
@@ -51,6 +58,7 @@ int usage(const char *msg) {
     std::fprintf(stderr,
                  "error: %s\nusage: pmsz <path>,<W>,<H>,<D> <abs_eb> <sz3|zfp> <PX> <PY> <PZ> [options]\n"
                  "       pmsz <path> <W> <H> <D> <abs_eb> <sz3|zfp> <PX> <PY> <PZ> [options]\n"
+                 "       pmsz --reconstruct <decp>,<W>,<H>,<D> <abs_eb> --out FILE [--deltas FILE] [--edits FILE]\n"
                  "options: --decp FILE  --dtype f64|f32  --q N  --max-sweeps N  --full-sweeps\n"
                  "         --out FILE   --verify  --cmp-size BYTES\n"
                  "         --naive      the naive-MSz strategy (the reference's naive_MSz program)\n",
@@ -85,11 +93,15 @@ int parse(int argc, char **argv, Args &a) {
         else if (s == "--full-sweeps") a.full = true;
         else if (s == "--verify") a.verify = true;
         else if (s == "--naive") a.naive = true;
+        else if (s == "--reconstruct") a.recon = true;
+        else if (s == "--deltas") { const char *v = need("file"); if (!v) return usage("--deltas needs a file"); a.deltas_file = v; }
+        else if (s == "--edits") { const char *v = need("file"); if (!v) return usage("--edits needs a file"); a.edits_file = v; }
         else if (s.size() > 2 && s[0] == '-' && s[1] == '-') return usage(("unknown option " + s).c_str());
         else pos.push_back(s);
     }
     size_t k = 0;
-    if (pos.size() == 6 && pos[0].find(',') != std::string::npos) {
+    const size_t npos_args = a.recon ? 2 : 6;  // after path,W,H,D: eb [comp PX PY PZ]
+    if (pos.size() == npos_args && pos[0].find(',') != std::string::npos) {
         // comma form: argv[1] = path,W,H,D (pMSz.cu:2655-2667)
         std::istringstream iss(pos[0]);
         std::string part;
@@ -99,7 +111,7 @@ int parse(int argc, char **argv, Args &a) {
             return usage("parsing error for dimensions");
         a.path = p[0];
         k = 1;
-    } else if (pos.size() == 9) {
+    } else if (pos.size() == npos_args + 3) {
         a.path = pos[0];
         if (!parse_size(pos[1], a.W) || !parse_size(pos[2], a.H) || !parse_size(pos[3], a.D))
             return usage("parsing error for dimensions");
@@ -110,6 +122,7 @@ int parse(int argc, char **argv, Args &a) {
     char *end = nullptr;
     a.eb = std::strtod(pos[k].c_str(), &end);
     if (!end || *end || !(a.eb > 0)) return usage("error bound must be a positive number");
+    if (a.recon) return a.out.empty() ? usage("--reconstruct needs --out FILE") : 0;
     a.comp = pos[k + 1];
     if (a.comp != "sz3" && a.comp != "zfp") return usage("compressor must be sz3 or zfp");
     a.px = std::atoi(pos[k + 2].c_str());
@@ -286,11 +299,68 @@ int run(const Args &a) {
     return st == PMSZ_OK ? 0 : 3;
 }
 
+bool read_bytes(const std::string &path, std::vector<uint8_t> &v) {
+    std::ifstream in(path, std::ios::binary | std::ios::ate);
+    if (!in) {
+        std::fprintf(stderr, "error: cannot open %s\n", path.c_str());
+        return false;
+    }
+    v.resize(static_cast<size_t>(in.tellg()));
+    in.seekg(0);
+    in.read(reinterpret_cast<char *>(v.data()), static_cast<std::streamsize>(v.size()));
+    return static_cast<bool>(in);
+}
+
+// --reconstruct: decompressed field + _deltas.bin + _edits.bin -> corrected field.
+template <typename T>
+int run_reconstruct(const Args &a) {
+    const size_t n = a.W * a.H * a.D;
+    std::vector<T> prev;
+    std::vector<uint8_t> blob_d, blob_e, deltas(n);
+    if (!read_raw<T>(a.path, prev, n) || !read_bytes(a.deltas_file, blob_d) || !read_bytes(a.edits_file, blob_e))
+        return 1;
+    void *vals = nullptr;
+    size_t nc = 0;
+    if (pmsz_decode_deltas(blob_d.data(), blob_d.size(), n, a.q, deltas.data()) ||
+        pmsz_decode_clamps(blob_e.data(), blob_e.size(), sizeof(T), &vals, &nc)) {
+        std::fprintf(stderr, "error: cannot decode the edit files: %s\n", pmsz_last_error());
+        return 1;
+    }
+    T *dprev = nullptr, *dclamp = nullptr;
+    uint8_t *dd = nullptr;
+    int st = PMSZ_ERR_CUDA;
+    if (cudaMalloc(&dprev, n * sizeof(T)) == cudaSuccess && cudaMalloc(&dd, n) == cudaSuccess &&
+        cudaMalloc(&dclamp, std::max<size_t>(nc, 1) * sizeof(T)) == cudaSuccess &&
+        cudaMemcpy(dprev, prev.data(), n * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess &&
+        cudaMemcpy(dd, deltas.data(), n, cudaMemcpyHostToDevice) == cudaSuccess &&
+        (nc == 0 || cudaMemcpy(dclamp, vals, nc * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess)) {
+        st = sizeof(T) == 4 ? pmsz_reconstruct_f32(reinterpret_cast<const float *>(dprev), dd, reinterpret_cast<const float *>(dclamp), nc, n, a.eb, a.q, reinterpret_cast<float *>(dprev), nullptr)
+                            : pmsz_reconstruct_f64(reinterpret_cast<const double *>(dprev), dd, reinterpret_cast<const double *>(dclamp), nc, n, a.eb, a.q, reinterpret_cast<double *>(dprev), nullptr);
+        if (st == PMSZ_OK && cudaMemcpy(prev.data(), dprev, n * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = PMSZ_ERR_CUDA;
+    }
+    pmsz_free(vals);
+    cudaFree(dprev);
+    cudaFree(dd);
+    cudaFree(dclamp);
+    if (st != PMSZ_OK) {
+        std::fprintf(stderr, "error: reconstruction failed (%s): %s\n", pmsz_strerror(st), pmsz_last_error());
+        return 1;
+    }
+    if (!write_file(a.out, reinterpret_cast<const uint8_t *>(prev.data()), n * sizeof(T))) {
+        std::fprintf(stderr, "error: cannot write %s\n", a.out.c_str());
+        return 1;
+    }
+    std::cout << "reconstructed " << n << " voxels (" << nc << " clamp values) into " << a.out << std::endl;
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
     Args a;
     const int rc = parse(argc, argv, a);
     if (rc) return rc;
+    if (a.recon) return a.f32 ? run_reconstruct<float>(a) : run_reconstruct<double>(a);
     return a.f32 ? run<float>(a) : run<double>(a);
 }

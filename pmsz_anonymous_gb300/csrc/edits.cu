@@ -340,13 +340,19 @@ __global__ void __launch_bounds__(256) k_recon_flags(const uint8_t *__restrict__
     const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
     const size_t i0 = base + static_cast<size_t>(threadIdx.x) * 8;
     uint32_t qm = 0, bad = 0;
+    uint8_t d8[8];
+    if (i0 + 8 <= n && (reinterpret_cast<uintptr_t>(deltas + i0) & 7) == 0) {  // one 8-byte load
+        const uint2 u = *reinterpret_cast<const uint2 *>(deltas + i0);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) d8[j] = static_cast<uint8_t>(((j < 4 ? u.x : u.y) >> ((j & 3) * 8)) & 0xFFu);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) d8[j] = i0 + j < n ? deltas[i0 + j] : uint8_t(0);
+    }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        if (i0 + j < n) {
-            const int d = deltas[i0 + j];
-            if (d == q) qm |= 1u << j;
-            bad += d > q;
-        }
+        if (d8[j] == q && i0 + j < n) qm |= 1u << j;
+        bad += d8[j] > q;
     }
     uint32_t word = qm << ((lane & 3) * 8);
     word |= __shfl_xor_sync(0xFFFFFFFFu, word, 1);
@@ -391,19 +397,31 @@ __global__ void __launch_bounds__(256) k_recon_apply(const T *prev, const uint8_
     }
     __syncthreads();
     const uint32_t t0 = tile_off[blockIdx.x];
+    // consecutive threads, consecutive voxels; all eight symbols and values
+    // are loaded before any is used, so their loads are in flight together
+    int d8[8];
+    T v8[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-        const uint32_t off = static_cast<uint32_t>(threadIdx.x) * 8 + j;
+        const size_t i = base + static_cast<size_t>(j) * 256 + threadIdx.x;
+        d8[j] = i < n ? deltas[i] : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const size_t i = base + static_cast<size_t>(j) * 256 + threadIdx.x;
+        v8[j] = i < n ? prev[i] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t off = static_cast<uint32_t>(j) * 256 + threadIdx.x;
         const size_t i = base + off;
         if (i >= n) break;
-        const int d = deltas[i];
-        T v;
-        if (d == q) {
+        T v = v8[j];
+        if (d8[j] == q) {
             const uint32_t w = off >> 5;
             v = clamp[t0 + s_pre[w] + __popc(s_fl[w] & ((1u << (off & 31)) - 1u))];
         } else {
-            v = prev[i];
-            for (int k = 0; k < d; ++k) v = v - delta;
+            for (int k = 0; k < d8[j]; ++k) v = v - delta;
         }
         out[i] = v;
     }

@@ -135,3 +135,28 @@ def test_cli_rejects_multi_rank_grids_and_bad_arguments(tmp_path):
     p = subprocess.run([exe, str(tmp_path / "missing.bin") + ",4,4,4", "1e-3", "sz3", "1", "1", "1"],
                        cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert p.returncode != 0
+
+
+def test_cli_reconstruct_rebuilds_the_corrected_field(cuda, tmp_path):
+    # correction with the CLI, then its decoder mode on the decompressed field
+    # and the two edit files: the corrected field, byte for byte
+    exe = _cli()
+    shape, eb = (24, 20, 28), 1e-3
+    f = F.perlin_field(shape, 37, 4, 1 / 16, dtype=np.float64)
+    fh = F.standin(f, eb, "zfp", 37)
+    path, decp, out, rec = (tmp_path / n for n in ("field.bin", "decp.bin", "corrected.bin", "rebuilt.bin"))
+    f.tofile(path)
+    fh.tofile(decp)
+    nz, ny, nx = shape
+    p = subprocess.run([exe, f"{path},{nx},{ny},{nz}", repr(eb), "zfp", "1", "1", "1", "--decp", str(decp),
+                        "--out", str(out)], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    p = subprocess.run([exe, "--reconstruct", f"{decp},{nx},{ny},{nz}", repr(eb), "--out", str(rec)], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert "reconstructed" in p.stdout
+    assert rec.read_bytes() == out.read_bytes()
+    assert rec.read_bytes() != decp.read_bytes()
+    p = subprocess.run([exe, "--reconstruct", f"{decp},{nx},{ny},{nz}", repr(eb), "--out", str(rec), "--deltas",
+                        str(tmp_path / "missing.bin")], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert p.returncode != 0
