@@ -63,6 +63,8 @@ def parse(argv=None):
     p.add_argument("--octaves", type=int, default=5)
     p.add_argument("--base", type=float, default=1 / 64)
     p.add_argument("--persistence", type=float, default=0.5)
+    p.add_argument("--cpu-single-slices", type=int, default=32,
+                   help="z-slices of the single-thread CPU sample (0 = none)")
     p.add_argument("--cpu-slices", type=int, default=0,
                    help="z-slices of the CPU sample (0 = the whole field: about 10 s on 16 cores at 512^3 fp64)")
     p.add_argument("--no-cpu", action="store_true")
@@ -354,6 +356,17 @@ def run_ours(args):
                                "sample": (f"the whole field ({cn} voxels)" if nsl == f.shape[0] else
                                           f"first {nsl} z-slices ({cn} voxels) of the same field") + ", "
                                          f"CPU oracle, {cdt:.2f} s"}
+        if args.cpu_single_slices > 0:  # the same oracle on one thread, on a slab of the field
+            from oracle import oracle as O
+            n1 = min(args.cpu_single_slices, f.shape[0])
+            O.set_threads(1)
+            try:
+                sn, sdt, _, ssw = cpu_sample(f[:n1].cpu().numpy(), fh0[:n1].cpu().numpy(), args.eb, n1)
+            finally:
+                O.set_threads(thr)
+            out["cpu_baseline"]["single_thread"] = {
+                "value": sn / sdt / 1e9, "unit": "Gvox/s", "cores": 1,
+                "sample": f"first {n1} z-slices ({sn} voxels) of the same field, {ssw} sweeps, CPU oracle, {sdt:.2f} s"}
     out["clocks"] = clk.summary()
     if world > 1:
         dist.barrier()

@@ -398,7 +398,12 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint64_t edits = 0;
     int status = PMSZ_ERR_NOT_CONVERGED;
     std::vector<SweepSlot> log;
-    const unsigned long long tail_at = std::max<unsigned long long>(g.n / 32, 1ull << 16);
+    // The cooperative tail takes over once the next active set is estimated
+    // below N/32, but never above kTailCap voxels: its barrier-separated
+    // phases serve millions of active voxels worse than list sweeps do, and at
+    // 1536^3 N/32 is 113 M.
+    constexpr unsigned long long kTailCap = 1ull << 20;
+    const unsigned long long tail_at = std::max<unsigned long long>(std::min<unsigned long long>(g.n / 32, kTailCap), 1ull << 16);
     if (use_list) {
         // Sweep 0 (the fused first pass and its edits) on the stream; then the
         // voxel-list sweeps as a CUDA graph whose while node repeats a body of
