@@ -172,3 +172,45 @@ def test_packed_delta_encoder_matches_symbol_encoder(lib):
         packed = O.pack_nbits(sym, nb)
         assert len(packed) == A.packed_len(sym.size, q)
         assert A.encode_packed_deltas(np.frombuffer(packed, np.uint8)) == A.encode_deltas(sym, q)
+
+
+def test_reconstruct_argument_errors_without_gpu(lib):
+    # checked before any CUDA call: null pointers, n, q and the error bound
+    buf = (ctypes.c_double * 8)()
+    sym = (ctypes.c_uint8 * 8)()
+    p, d = ctypes.addressof(buf), ctypes.addressof(sym)
+    assert lib.pmsz_reconstruct_f64(None, d, None, 0, 8, 1e-3, 5, p, None) == capi.PMSZ_ERR_ARG
+    assert lib.pmsz_reconstruct_f64(p, d, None, 3, 8, 1e-3, 5, p, None) == capi.PMSZ_ERR_ARG  # clamps without a list
+    assert lib.pmsz_reconstruct_f64(p, d, None, 0, 0, 1e-3, 5, p, None) == capi.PMSZ_ERR_ARG
+    assert lib.pmsz_reconstruct_f64(p, d, None, 0, 8, 1e-3, 0, p, None) == capi.PMSZ_ERR_ARG
+    assert lib.pmsz_reconstruct_f32(p, d, None, 0, 8, -1.0, 5, p, None) == capi.PMSZ_ERR_ARG
+    assert b"error bound" in lib.pmsz_last_error()
+
+
+def _cli_run(args, cwd):
+    import subprocess
+    _build.build()
+    exe = os.path.join(os.path.dirname(_build.__file__), "lib", "pmsz")
+    return subprocess.run([exe] + args, cwd=cwd, capture_output=True, text=True, timeout=60)
+
+
+def test_cli_argument_errors_without_gpu(tmp_path):
+    # every one of these fails in argument parsing or file reading, before
+    # any CUDA call
+    p = _cli_run(["x.bin,4,4,4", "1e-3", "sz3", "2", "1", "1"], tmp_path)
+    assert p.returncode == 2 and "PX PY PZ" in p.stderr
+    p = _cli_run(["x.bin,4,4,4", "-1", "sz3", "1", "1", "1"], tmp_path)
+    assert p.returncode == 2 and "error bound" in p.stderr
+    p = _cli_run(["x.bin,4,4,4", "1e-3", "lz4", "1", "1", "1"], tmp_path)
+    assert p.returncode == 2 and "compressor" in p.stderr
+    p = _cli_run(["--reconstruct", "x.bin,4,4,4", "1e-3"], tmp_path)
+    assert p.returncode == 2 and "--out" in p.stderr
+    p = _cli_run(["--reconstruct", "x.bin,4,4", "1e-3", "--out", "r.bin"], tmp_path)
+    assert p.returncode == 2 and "dimensions" in p.stderr
+    p = _cli_run(["--reconstruct", str(tmp_path / "missing.bin") + ",4,4,4", "1e-3", "--out", "r.bin"], tmp_path)
+    assert p.returncode == 1 and "cannot open" in p.stderr
+    np.zeros(64).tofile(tmp_path / "decp.bin")
+    p = _cli_run(["--reconstruct", str(tmp_path / "decp.bin"), "4", "4", "4", "1e-3", "--out", "r.bin",
+                  "--deltas", str(tmp_path / "none.bin")], tmp_path)
+    assert p.returncode == 1 and "none.bin" in p.stderr
+    assert not (tmp_path / "r.bin").exists()
