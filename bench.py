@@ -69,9 +69,10 @@ def parse(argv=None):
                    help="z-slices of the CPU sample (0 = the whole field: about 10 s on 16 cores at 512^3 fp64)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
-    p.add_argument("--workload", choices=["plain", "batch", "serve"], default="plain",
+    p.add_argument("--workload", choices=["plain", "batch", "serve", "reconstruct"], default="plain",
                    help="plain: one 512^3 field (the headline); batch: 64 mixed fp32 fields; "
-                        "serve: Poisson job stream through the correction server")
+                        "serve: Poisson job stream through the correction server; "
+                        "reconstruct: the decoder on the plain workload's field")
     p.add_argument("--serve-jobs", type=int, default=120)
     p.add_argument("--serve-rates", default="100,300,1000,3000", help="arrival rates (jobs/s) to sweep")
     p.add_argument("--batch-fields", type=int, default=64)
@@ -464,6 +465,57 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_reconstruct(args):
+    """Decoder form: the corrected field rebuilt from the decompressed field,
+    the delta symbols and the clamp list (pmsz_reconstruct_*), on the plain
+    workload's field; correction and extraction are untimed setup."""
+    import torch
+    from pmsz_anonymous_gb300 import _build, api
+    _build.build()
+    dev = torch.device("cuda", 0)
+    dtype = torch.float64 if args.dtype == "f64" else torch.float32
+    f, prev = gen_fields(args, torch, dev, dtype)
+    cur = prev.clone()
+    api.correct(f, cur, args.eb)
+    deltas, clamp, _ = api.extract_edits(prev, cur, f, args.eb)
+    out = torch.empty_like(prev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MB > L2 between steps
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        api.reconstruct(prev, deltas, clamp, args.eb, out=out)
+    ts = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        start.record()
+        api.reconstruct(prev, deltas, clamp, args.eb, out=out)
+        stop.record()
+        stop.synchronize()
+        ts.append(start.elapsed_time(stop))
+    ok = torch.equal(out.view(torch.uint8), cur.view(torch.uint8))
+    n = prev.numel()
+    ms = statistics.mean(ts)
+    item = prev.element_size()
+    peak, kind = measured_peaks()
+    algo = n * (2 * item + 1) + clamp.numel() * item
+    wl = workload_config(args)["workload"].replace("plain single-field correction", "reconstruction from the edit output")
+    print(json.dumps({
+        "metric": "Gvox/s reconstruction (decompressed field + delta symbols + clamp list -> corrected field)",
+        "value": n / (ms * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+        "data": "synthetic",
+        "config": {"workload": wl, "voxels": n, "clamps": clamp.numel(), "l2": "256 MB written between steps",
+                   "bit_exact_with_the_correction": ok},
+        "roofline": {"bound": "hbm", "kernel": "pmsz_reconstruct call (flags, tile scan, host count check, k_recon_apply)",
+                     "achieved": algo / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": algo / (ms * 1e-3) / 1e9 / peak, "peak_kind": f"{kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": algo},
+        "gpu_launches": 3 * args.steps,
+    }), flush=True)
+    if not ok:
+        raise SystemExit("reconstruction differs from the corrected field")
+
+
 def serve_specs(count: int, base_seed: int = 1000):
     """Served stream: per-job seed base+id, 3-6 octaves, each axis log-uniform
     in 32..384, 70% fp32 / 30% fp64, eps log-uniform in [1e-5, 1e-2], sz3 /
@@ -548,6 +600,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "reconstruct":
+        run_reconstruct(args)
     else:
         run_ours(args)
 
