@@ -214,3 +214,15 @@ def test_cli_argument_errors_without_gpu(tmp_path):
                   "--deltas", str(tmp_path / "none.bin")], tmp_path)
     assert p.returncode == 1 and "none.bin" in p.stderr
     assert not (tmp_path / "r.bin").exists()
+
+
+def test_python_api_rejects_host_tensors_without_gpu():
+    # the Python layer checks its tensors before any CUDA call
+    torch = pytest.importorskip("torch")
+    from pmsz_anonymous_gb300 import api
+    f = torch.zeros((4, 4, 4), dtype=torch.float64)
+    d = torch.zeros(64, dtype=torch.uint8)
+    with pytest.raises(TypeError):
+        api.reconstruct(f, d, torch.zeros(0, dtype=torch.float64), 1e-3)
+    with pytest.raises(TypeError):
+        api.correct(f, f.clone(), 1e-3)
