@@ -12,19 +12,26 @@ value   device-resident throughput, Gvox/s = N / (device time of one
 e2e     the same through the host-buffer C ABI (pmsz_correct_host_*): pinned
         host f and fhat copied in, the correction, the edit extraction and the
         copy back of what the reference's main hands to its host encoder --
-        the delta symbols (1 B/voxel) and the clamp list -- all timed.
+        the delta symbols (packed at 3 bits) and the clamp list -- all timed.
 roofline  the fused labelling + first detection pass k_tiled<T,kFirst> (the
-        largest kernel, about 40 % of a call): algorithmic bytes
-        2*N*(sizeof(T)+1) -- the one-time original labelling (read f, write
-        the code byte) plus one detection sweep (read fhat and the code byte)
-        -- over its event-timed duration, against the measured HBM copy
-        bandwidth; traffic = ncu dram bytes per launch of the same kernel.
+        largest kernel): algorithmic bytes 2*N*(sizeof(T)+1) -- the one-time
+        original labelling (read f, write the code byte) plus one detection
+        sweep (read fhat and the code byte) -- over its event-timed duration,
+        against the measured HBM copy bandwidth; traffic = ncu dram bytes per
+        launch of the same kernel.  roofline.per_step: the whole step's
+        active-set algorithmic bytes over ms_per_step.
 cpu_baseline  the CPU oracle (a restatement of the reference loop, OpenMP on
-        all host cores) on a z-slab sample of the same field.
+        all host cores) on the whole field; parity: its corrected field, sweep
+        count and per-sweep counters against the GPU's, bit for bit.
+batch / serve / reference_kernels  (after the timed region) the batched form
+        on 64 mixed fp32 fields against the same fields one by one, the
+        served stream's jobs/s and p50/p99 at three arrival rates, and the
+        reference's own CUDA kernels timed beside this library on the field.
 
 --impl reference: the reference's path on the host cores -- the reference
 itself is CUDA-only with no CPU implementation, so this arm runs the CPU
-oracle restatement (kind "port") on the same slab sample.
+oracle restatement (kind "port") on the whole field, generated on the host
+cores by the oracle library (no GPU code is loaded).
 With N > 1 (torchrun) every rank corrects its own replica: no data-path
 collective; a barrier brackets the timed region and the max over ranks is taken.
 """
@@ -76,6 +83,8 @@ def parse(argv=None):
     p.add_argument("--serve-jobs", type=int, default=120)
     p.add_argument("--serve-rates", default="100,300,1000,3000", help="arrival rates (jobs/s) to sweep")
     p.add_argument("--batch-fields", type=int, default=64)
+    p.add_argument("--no-extra", action="store_true",
+                   help="plain workload only: skip the batch, serve and reference-kernel legs")
     return p.parse_args(argv)
 
 
@@ -173,15 +182,26 @@ def profiled_traffic(name: str):
 
 def cpu_sample(f: np.ndarray, fh: np.ndarray, eb: float, slices: int):
     """Time the CPU oracle on the first `slices` z-slices of the field (0 =
-    all of it)."""
+    all of it).  Returns (voxels, seconds, threads, sweeps, (corrected field,
+    status, per-sweep records))."""
     from oracle import oracle as O
     slices = slices or f.shape[0]
     fs = np.ascontiguousarray(f[:slices])
     fhs = np.ascontiguousarray(fh[:slices])
     t0 = time.perf_counter()
-    _, _, st, sweeps, _ = O.correct(fs, fhs, eb)
+    out, _, st, sweeps, recs = O.correct(fs, fhs, eb)
     dt = time.perf_counter() - t0
-    return fs.size, dt, O.num_threads(), sweeps
+    return fs.size, dt, O.num_threads(), sweeps, (out, st, recs)
+
+
+def host_fields(args):
+    """f and fhat of the workload generated on the host cores by the oracle
+    library (bit-identical to the GPU generator; loads no GPU code)."""
+    from oracle import oracle as O
+    nx, ny, nz = (int(v) for v in args.shape.split(","))
+    dt = np.float64 if args.dtype == "f64" else np.float32
+    f = O.perlin_field((nz, ny, nx), args.seed, args.octaves, args.base, args.persistence, 2.0, dtype=dt)
+    return f, O.standin(f, args.eb, args.comp, args.seed)
 
 
 def gen_fields(args, torch, device, dtype):
@@ -208,38 +228,36 @@ def workload_config(args, extra=None):
 
 
 def run_reference(args):
+    """The reference's path on the host cores: the reference is CUDA-only, so
+    its CPU implementation is the oracle's restatement of c_loops (kind
+    "port"), on the whole field the GPU arm corrects, with every host thread.
+    Inputs come from the oracle's host generator: nothing here loads the
+    CUDA library or initialises a GPU."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import torch
-    dtype = torch.float64 if args.dtype == "f64" else torch.float32
-    f, fh = gen_fields(args, torch, torch.device("cuda:0"), dtype)
-    nz = f.shape[0]
-    fall, fhall = f.cpu().numpy(), fh.cpu().numpy()
-    del f, fh
-    nsl = args.cpu_slices
-    if not nsl:  # size the slab so the whole K + W run takes about two minutes
-        probe = min(nz, 16)
-        _, pdt, _, _ = cpu_sample(fall, fhall, args.eb, probe)
-        nsl = int(max(probe, min(nz, 120.0 / (args.steps + args.warmup) / (pdt / probe))))
+    fall, fhall = host_fields(args)
+    nz = fall.shape[0]
+    nsl = args.cpu_slices or nz
     whole = nsl == nz
-    fs, fhs = fall[:nsl], fhall[:nsl]
-    times, n, thr = [], 0, 0
+    times, n, thr, sweeps = [], 0, 0, 0
     for i in range(args.warmup + args.steps):
-        n, dt, thr, sweeps = cpu_sample(fs, fhs, args.eb, nsl)
+        n, dt, thr, sweeps, _ = cpu_sample(fall, fhall, args.eb, nsl)
         if i >= args.warmup:
             times.append(dt)
     v = n / statistics.mean(times) / 1e9
     sample = (f"the whole field ({n} voxels)" if whole else f"first {nsl} z-slices ({n} voxels) of the field") + \
-        ", CPU oracle restatement"
+        f", CPU oracle restatement, {sweeps} sweeps"
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Gvox/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
-        "data": "synthetic", "config": workload_config(args, {"sample": sample}),
+        "data": "synthetic", "config": workload_config(args, {"sample": sample, "same_config": whole}),
         "cpu_baseline": {"value": v, "unit": "Gvox/s", "cores": thr, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "Gvox/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference's path is CUDA-only; its CPU arm is the oracle restatement of c_loops",
+        "gpu_launches": 0,
+        "note": "the reference's path is CUDA-only; its CPU arm is the oracle restatement of c_loops "
+                "(pMSz.cu:1872-2074), inputs from the oracle's host generator",
     }), flush=True)
 
 
@@ -348,27 +366,69 @@ def run_ours(args):
         "gpu_launches": launches,
         "verify": ok,
     }
+    # active-set algorithmic bytes of the whole step (one-time labelling, each
+    # sweep's examined voxels, each edit), and the same with every sweep
+    # counted as a full sweep (what the reference's schedule would move)
+    act = [int(v) for v in last.log[:, 6]]
+    req = [int(v) for v in last.log[:, 3]]
+    step_bytes = n * (itemsize + 1) + sum(act) * (itemsize + 1) + sum(req) * (3 * itemsize + 2)
+    full_bytes = n * (itemsize + 1) + len(act) * n * (itemsize + 1) + sum(req) * (3 * itemsize + 2)
+    out["roofline"]["per_step"] = {
+        "algorithmic_bytes": step_bytes, "achieved": step_bytes / (ms * 1e-3) / 1e9,
+        "frac": step_bytes / (ms * 1e-3) / 1e9 / peak,
+        "what": "N*(s+1) labelling + sum over sweeps of examined voxels*(s+1) + edits*(3s+2), s = sizeof(T), "
+                "over ms_per_step"}
+    out["roofline"]["full_sweep_equivalent"] = {
+        "algorithmic_bytes": full_bytes, "achieved": full_bytes / (ms * 1e-3) / 1e9,
+        "what": "every sweep counted as a full sweep of N*(s+1) bytes (the reference's schedule); credits "
+                "skipped work, not a roofline fraction"}
     if rank == 0 and not args.no_cpu:
         nsl = args.cpu_slices or f.shape[0]
         fs = f[:nsl].cpu().numpy()
         fhs = fh0[:nsl].cpu().numpy()
-        cn, cdt, thr, _ = cpu_sample(fs, fhs, args.eb, nsl)
+        cn, cdt, thr, csw, (cfield, cst, crecs) = cpu_sample(fs, fhs, args.eb, nsl)
         out["cpu_baseline"] = {"value": cn / cdt / 1e9, "unit": "Gvox/s", "cores": thr, "kind": "port",
                                "sample": (f"the whole field ({cn} voxels)" if nsl == f.shape[0] else
                                           f"first {nsl} z-slices ({cn} voxels) of the same field") + ", "
                                          f"CPU oracle, {cdt:.2f} s"}
+        # parity: the oracle's corrected field against the GPU's, bit for bit
+        if nsl == f.shape[0]:
+            gfield, gres = fh, last
+        else:
+            gfield = fh0[:nsl].clone()
+            gres = api.correct(f[:nsl].contiguous(), gfield, args.eb)
+        gnp = gfield.cpu().numpy()
+        bits = np.uint64 if itemsize == 8 else np.uint32
+        out["parity"] = {
+            "checked_against": "CPU oracle (restatement of c_loops, pinned to the reference's kernels)",
+            "voxels": int(cn),
+            "bit_exact": bool(np.array_equal(gnp.view(np.uint8), cfield.view(np.uint8))),
+            "voxels_differing": int(np.count_nonzero(gnp.view(bits) != cfield.view(bits))),
+            "sweeps_equal": bool(gres.sweeps == csw), "status_equal": bool(gres.status == cst),
+            "records_equal": bool(np.array_equal(gres.log[:, :5], crecs)),
+            "sweeps": int(csw)}
+        del gnp, cfield
         if args.cpu_single_slices > 0:  # the same oracle on one thread, on a slab of the field
             from oracle import oracle as O
             n1 = min(args.cpu_single_slices, f.shape[0])
             O.set_threads(1)
             try:
-                sn, sdt, _, ssw = cpu_sample(f[:n1].cpu().numpy(), fh0[:n1].cpu().numpy(), args.eb, n1)
+                sn, sdt, _, ssw, _ = cpu_sample(f[:n1].cpu().numpy(), fh0[:n1].cpu().numpy(), args.eb, n1)
             finally:
                 O.set_threads(thr)
             out["cpu_baseline"]["single_thread"] = {
                 "value": sn / sdt / 1e9, "unit": "Gvox/s", "cores": 1,
                 "sample": f"first {n1} z-slices ({sn} voxels) of the same field, {ssw} sweeps, CPU oracle, {sdt:.2f} s"}
     out["clocks"] = clk.summary()
+    if rank == 0 and not args.no_extra:
+        # the rest of the metric: batched vox/s, served p50/p99, and the
+        # reference's own CUDA kernels on this GPU (untimed legs after the
+        # timed region; none of them changes `value`)
+        del fh, fh0
+        torch.cuda.empty_cache()
+        out["batch"] = batch_measure(args, steps=5, warmup=3)
+        out["serve"] = serve_measure(args, rates=[100.0, 1000.0, 3000.0])
+        out["reference_kernels"] = reference_kernels_measure(args)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -390,9 +450,10 @@ def batch_specs(count: int, base_seed: int = 100):
     return specs
 
 
-def run_batch(args):
+def batch_measure(args, steps: int, warmup: int) -> dict:
     """Batched form: all fields in one pmsz_correct_batch call vs the same
-    fields corrected one by one with pmsz_correct_f32."""
+    fields corrected one by one with pmsz_correct_f32; the batch's fields are
+    checked bit for bit against the one-by-one fields."""
     import torch
     from pmsz_anonymous_gb300 import _build, api
     _build.build()
@@ -432,11 +493,11 @@ def run_batch(args):
 
     times = {}
     for name, fn in (("plain", one_by_one), ("batch", batched)):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             refresh()
             fn()
         ts = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             refresh()
             torch.cuda.synchronize()
             start.record()
@@ -446,11 +507,17 @@ def run_batch(args):
             ts.append(start.elapsed_time(stop))
         times[name] = statistics.mean(ts)
     refresh()
+    alone = [api.correct(f, w, eb) for w, (f, _, eb) in zip(work, fields)]
+    alone_fields = [w.clone() for w in work]
+    refresh()
     res = api.correct_batch([(f, w, eb) for w, (f, _, eb) in zip(work, fields)])
-    out = {
+    same = all(torch.equal(a.view(torch.int32), w.view(torch.int32)) for a, w in zip(alone_fields, work))
+    same_sweeps = all(a.sweeps == r.sweeps and a.status == r.status for a, r in zip(alone, res))
+    del alone_fields
+    return {
         "metric": "batched vox/s (64 mixed fp32 fields, one pmsz_correct_batch call)",
-        "value": nvox / (times["batch"] * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": times["batch"], "higher_is_better": True, "scaling": "weak",
+        "value": nvox / (times["batch"] * 1e-3) / 1e9, "unit": "Gvox/s", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": times["batch"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{len(specs)} fp32 Perlin fBm fields (seeds {specs[0][0]}-{specs[-1][0]}, 4 octaves, "
                                "base 1/32), axes uniform 32-256, eps log-uniform [1e-5,1e-2], half sz3 / half zfp "
@@ -460,9 +527,13 @@ def run_batch(args):
         "batch_over_plain": times["plain"] / times["batch"],
         "statuses": sorted(set(r.status for r in res)),
         "sweeps_max": max(r.sweeps for r in res),
+        "bit_exact_with_one_by_one": bool(same), "sweeps_equal_one_by_one": bool(same_sweeps),
         "autotune": tune_summary,
     }
-    print(json.dumps(out), flush=True)
+
+
+def run_batch(args):
+    print(json.dumps(batch_measure(args, args.steps, args.warmup)), flush=True)
 
 
 def run_reconstruct(args):
@@ -530,7 +601,7 @@ def serve_specs(count: int, base_seed: int = 1000):
     return out
 
 
-def run_serve(args):
+def serve_measure(args, rates) -> dict:
     """Continuous-batching server under Poisson arrivals at swept rates."""
     import threading
     import torch
@@ -548,7 +619,7 @@ def run_serve(args):
     nvox = sum(f.numel() for f, _, _ in jobs)
     rows = []
     rng = np.random.RandomState(7)
-    for rate in [float(r) for r in args.serve_rates.split(",")]:
+    for rate in rates:
         for w, (_, fh, _) in zip(work, jobs):
             w.copy_(fh)
         torch.cuda.synchronize()
@@ -583,13 +654,38 @@ def run_serve(args):
                      "queue_p99_ms": float(np.percentile([i["queue_ms"] for i in infos], 99)),
                      "ok": int(sum(i["status"] == 0 for i in infos))})
     best = max(rows, key=lambda r: r["jobs_s"])
-    print(json.dumps({
+    return {
         "metric": "served correction stream: jobs/s and p50/p99 latency", "value": best["jobs_s"], "unit": "jobs/s",
         "n_gpus": 1, "higher_is_better": True, "dtype": "f32/f64", "data": "synthetic",
         "config": {"workload": f"{len(jobs)} jobs, Poisson arrivals, axes log-uniform 32-384, 70% fp32 / 30% fp64, "
                                "3-6 octaves, eps log-uniform [1e-5,1e-2], sz3/zfp stand-ins 50/50, 120 GB budget",
                    "voxels": nvox},
-        "rates": rows}), flush=True)
+        "rates": rows}
+
+
+def run_serve(args):
+    print(json.dumps(serve_measure(args, [float(r) for r in args.serve_rates.split(",")])), flush=True)
+
+
+def reference_kernels_measure(args) -> dict:
+    """The reference's own CUDA kernels (pMSz.cu compiled unmodified for
+    sm_103a) driven through its c_loops host sequence at an MPI grid of
+    1x1x1 on this GPU, beside this library on the same field
+    (oracle/time_reference.py, a separate process).  fp64 only: the
+    reference hard-codes double."""
+    if args.dtype != "f64":
+        return {"unavailable": "the reference's kernels are fp64 only"}
+    cmd = [sys.executable, os.path.join(ROOT, "oracle", "time_reference.py"), "--shape", args.shape,
+           "--eb", repr(args.eb), "--comp", args.comp, "--seed", str(args.seed), "--octaves", str(args.octaves),
+           "--base", repr(args.base), "--runs", "2"]
+    try:
+        p = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": "time_reference.py did not finish within 900 s"}
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    if p.returncode != 0 or not lines:
+        return {"unavailable": f"time_reference.py exited {p.returncode}: {p.stderr.strip()[-300:]}"}
+    return json.loads(lines[-1])
 
 
 def main():

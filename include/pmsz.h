@@ -173,12 +173,16 @@ int pmsz_correct_naive_f64(const double *f, double *fhat, size_t nx, size_t ny, 
  * exits.  Limits, rejected with PMSZ_ERR_ARG and a message: nx*ny*nz <=
  * PMSZ_NOALLOC_MAX_VOXELS (2^21, e.g. 128^3), ceil(nx/32)*ny*nz <=
  * PMSZ_NOALLOC_MAX_WORDS, max_sweeps <= PMSZ_NOALLOC_MAX_SWEEPS (also the
- * default).  The first call on a device looks up the array's device address
- * with that device current; make that first call before any stream capture.
- * All calls on a device share the array and every call clears what must
- * start at zero, so calls that overlap on the GPU (two streams, or two host
- * threads) race: serialise them.  PMSZ_FLAG_TIMING is ignored; the ms_*
- * fields of res are set to 0.
+ * default).  Every call looks up the array's device address in the calling
+ * thread's current context (cudaGetSymbolAddress, no allocation), so the
+ * address stays right after cudaDeviceReset or in another context; the
+ * first call in a context also loads the library's device code there, so
+ * make it before any stream capture.  All calls on a device share the
+ * array and every call clears what must start at zero, so calls that
+ * overlap on the GPU (two streams, or two host threads) race: serialise
+ * them.  PMSZ_FLAG_TIMING is ignored: ms_first_pass, ms_detect and ms_apply
+ * are 0; ms_total is the host clock over the loop, which synchronises the
+ * stream after every sweep.
  */
 #define PMSZ_NOALLOC_MAX_VOXELS 2097152u
 #define PMSZ_NOALLOC_MAX_WORDS 131072u

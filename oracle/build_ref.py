@@ -1,7 +1,8 @@
 """Build recipe of the reference-kernel harness (test infrastructure only).
 
 * ``oracle/_ref/pmsz_ref.cubin`` -- the UNMODIFIED reference ``pMSz.cu``,
-  compiled where it lies (``/root/reference``) into sm_103a device code, with
+  compiled where it lies (``$PMSZ_REFERENCE_DIR``, by default
+  ``/root/reference``) into sm_103a device code, with
   the declaration-only headers of ``oracle/ref_shim`` standing in for MPI,
   SZ3, ZFP and zstd (the cubin keeps only the kernels; nothing of those
   libraries is called).  Built only where the reference sources exist; the
@@ -22,9 +23,12 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/pMSz.cu"
+# where the reference's sources lie: $PMSZ_REFERENCE_DIR, by default the
+# read-only checkout at /root/reference
+REF_DIR = os.environ.get("PMSZ_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_DIR, "pMSz.cu")
 CUBIN = os.path.join(OUT, "pmsz_ref.cubin")
-NAIVE_SRC = "/root/reference/naive_MSz.cu"
+NAIVE_SRC = os.path.join(REF_DIR, "naive_MSz.cu")
 NAIVE_CUBIN = os.path.join(OUT, "naive_ref.cubin")
 HARNESS = os.path.join(OUT, "ref_harness")
 

@@ -66,6 +66,9 @@ def lib():
                     _P, _P, _I64, _I64, _I64, ctypes.c_double, ctypes.c_int, _I64, _P, _P, _P]
                 getattr(L, f"pmszo_reconstruct_{suf}").argtypes = [
                     _P, _P, _P, _I64, _I64, ctypes.c_double, ctypes.c_int, _P]
+                getattr(L, f"pmszo_perlin_{suf}").argtypes = [_P, _I64, _I64, _I64, _P, _P, _P, ctypes.c_int]
+                getattr(L, f"pmszo_standin_{suf}").argtypes = [_P, _P, _I64, ctypes.c_double, ctypes.c_int,
+                                                               ctypes.c_uint64]
             L.pmszo_path_compress.argtypes = [_P, _P, _I64]
             L.pmszo_pack_nbits.argtypes = [_P, _I64, ctypes.c_uint, _P]
             L.pmszo_pack_nbits.restype = ctypes.c_int64
@@ -230,3 +233,36 @@ def unpack_nbits(packed: bytes, n: int, nbits: int) -> np.ndarray:
 
 def bits_for_max(m: int) -> int:
     return int(lib().pmszo_bits_for_max(int(m)))
+
+
+def perlin_field(shape, seed: int, octaves: int, base_freq: float, persistence: float = 0.5,
+                 lacunarity: float = 2.0, dtype=np.float32) -> np.ndarray:
+    """Normalised Perlin fBm field of shape (nz, ny, nx) on the host cores,
+    bit-identical to pmsz_anonymous_gb300.fields.perlin_field (the noise of
+    generate_perlin.py:17-59, its permutation recipe :105-108)."""
+    from pmsz_anonymous_gb300 import fields  # numpy only: permutation and octave table
+    nz, ny, nx = (int(v) for v in shape)
+    out = np.empty((nz, ny, nx), dtype=dtype)
+    perm = np.ascontiguousarray(fields.permutation(seed), dtype=np.int32)
+    amps, freqs = fields.octave_table(octaves, base_freq, persistence, lacunarity)
+    amps, freqs = np.ascontiguousarray(amps), np.ascontiguousarray(freqs)
+    rc = getattr(lib(), f"pmszo_perlin_{_suf(out)}")(_ptr(out), nx, ny, nz, _ptr(perm), _ptr(amps), _ptr(freqs),
+                                                      int(octaves))
+    if rc != OK:
+        raise ValueError(f"perlin failed: {rc}")
+    return out
+
+
+def standin(f: np.ndarray, eb: float, compressor: str, seed: int = 0) -> np.ndarray:
+    """The labelled compressor stand-in of fields.standin on the host cores
+    ("sz3": plateaus, "zfp": bounded noise), bit-identical to it."""
+    kinds = {"sz3": 0, "zfp": 1}
+    if compressor not in kinds:
+        raise ValueError(f"unknown compressor {compressor!r} (expected 'sz3' or 'zfp')")
+    f = np.ascontiguousarray(f)
+    out = np.empty_like(f)
+    rc = getattr(lib(), f"pmszo_standin_{_suf(f)}")(_ptr(f), _ptr(out), f.size, float(eb), kinds[compressor],
+                                                     int(seed) & 0xFFFFFFFFFFFFFFFF)
+    if rc != OK:
+        raise ValueError(f"standin failed: {rc}")
+    return out

@@ -666,3 +666,117 @@ static int64_t pmszo_walk_as(const int64_t *oasc, const int64_t *odesc, const in
 
 PMSZO_DEFINE_NAIVE(float, f32)
 PMSZO_DEFINE_NAIVE(double, f64)
+
+/* ---------------------------------------------------------------------- */
+/* Synthetic inputs for the CPU legs of the benchmark, so that they need no */
+/* GPU and load nothing but this library.  The same bits as the numpy      */
+/* generator (pmsz_anonymous_gb300/fields.py) and the CUDA one: improved   */
+/* Perlin noise as generate_perlin.py:17-59 writes it (quintic fade, the   */
+/* 16-case gradient hash, a 512-entry permutation made by the caller as    */
+/* generate_perlin.py:105-108 makes it), summed over octaves with the      */
+/* caller's amplitudes and frequencies, then min-max normalised in double  */
+/* and cast to T.  Every operation is one IEEE double operation            */
+/* (-ffp-contract=off), as numpy evaluates the same expressions.           */
+/* ---------------------------------------------------------------------- */
+static inline double pmszo_fade(double t) { return t * t * t * (t * (t * 6.0 - 15.0) + 10.0); }
+static inline double pmszo_lerp(double a, double b, double t) { return a + t * (b - a); }
+static inline double pmszo_grad(int h, double x, double y, double z) {
+    h &= 15;
+    const double u = h < 8 ? x : y;
+    const double v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+}
+static double pmszo_perlin(double x, double y, double z, const int32_t *p) {
+    const double fx = floor(x), fy = floor(y), fz = floor(z);
+    const int X = (int)((int64_t)fx & 255), Y = (int)((int64_t)fy & 255), Z = (int)((int64_t)fz & 255);
+    x = x - fx;
+    y = y - fy;
+    z = z - fz;
+    const double u = pmszo_fade(x), v = pmszo_fade(y), w = pmszo_fade(z);
+    const int A = p[X] + Y, AA = p[A] + Z, AB = p[A + 1] + Z;
+    const int B = p[X + 1] + Y, BA = p[B] + Z, BB = p[B + 1] + Z;
+    return pmszo_lerp(
+        pmszo_lerp(pmszo_lerp(pmszo_grad(p[AA], x, y, z), pmszo_grad(p[BA], x - 1.0, y, z), u),
+                   pmszo_lerp(pmszo_grad(p[AB], x, y - 1.0, z), pmszo_grad(p[BB], x - 1.0, y - 1.0, z), u), v),
+        pmszo_lerp(pmszo_lerp(pmszo_grad(p[AA + 1], x, y, z - 1.0), pmszo_grad(p[BA + 1], x - 1.0, y, z - 1.0), u),
+                   pmszo_lerp(pmszo_grad(p[AB + 1], x, y - 1.0, z - 1.0),
+                              pmszo_grad(p[BB + 1], x - 1.0, y - 1.0, z - 1.0), u), v),
+        w);
+}
+static inline double pmszo_fbm(const int32_t *perm, const double *amps, const double *freqs, int octaves,
+                               int64_t x, int64_t y, int64_t z) {
+    double total = 0.0;
+    for (int o = 0; o < octaves; ++o) {
+        const double fr = freqs[o];
+        total = total + amps[o] * pmszo_perlin((double)x * fr, (double)y * fr, (double)z * fr, perm);
+    }
+    return total;
+}
+
+/* Two passes (range, then recompute and normalise), so no double copy of  */
+/* the field is held: a 1536^3 fp32 field needs only its own 13.5 GB.      */
+#define PMSZO_DEFINE_PERLIN(T, SUF)                                                              \
+    int pmszo_perlin_##SUF(T *out, int64_t nx, int64_t ny, int64_t nz, const int32_t *perm,      \
+                           const double *amps, const double *freqs, int octaves) {               \
+        if (nx <= 0 || ny <= 0 || nz <= 0 || octaves < 1 || !out || !perm) return PMSZO_ERR_ARG; \
+        for (int i = 0; i < 512; ++i)                                                            \
+            if (perm[i] < 0 || perm[i] > 255) return PMSZO_ERR_ARG;                              \
+        double mn = INFINITY, mx = -INFINITY;                                                    \
+        _Pragma("omp parallel for schedule(static) reduction(min:mn) reduction(max:mx)")         \
+        for (int64_t z = 0; z < nz; ++z)                                                         \
+            for (int64_t y = 0; y < ny; ++y)                                                     \
+                for (int64_t x = 0; x < nx; ++x) {                                               \
+                    const double v = pmszo_fbm(perm, amps, freqs, octaves, x, y, z);             \
+                    mn = v < mn ? v : mn;                                                        \
+                    mx = v > mx ? v : mx;                                                        \
+                }                                                                                \
+        const double range = mx - mn;                                                            \
+        _Pragma("omp parallel for schedule(static)")                                             \
+        for (int64_t z = 0; z < nz; ++z)                                                         \
+            for (int64_t y = 0; y < ny; ++y)                                                     \
+                for (int64_t x = 0; x < nx; ++x)                                                 \
+                    out[x + nx * (y + ny * z)] =                                                 \
+                        (T)((pmszo_fbm(perm, amps, freqs, octaves, x, y, z) - mn) / range);      \
+        return PMSZO_OK;                                                                         \
+    }
+
+PMSZO_DEFINE_PERLIN(float, f32)
+PMSZO_DEFINE_PERLIN(double, f64)
+
+/* The two labelled compressor stand-ins of fields.py: kind 0, SZ-like      */
+/* plateaus fhat = (2 eb) * rint(f / (2 eb)) (rint and numpy's round both   */
+/* round half to even); kind 1, ZFP-like noise fhat = f + eb * u with u in  */
+/* [-1, 1) from splitmix64 of (index ^ seed << 40).  A voxel with           */
+/* |f - fhat| > eps in T falls back to f.                                   */
+static inline uint64_t pmszo_splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+#define PMSZO_DEFINE_STANDIN(T, SUF, FABS)                                                       \
+    int pmszo_standin_##SUF(const T *f, T *fh, int64_t n, double eb, int kind, uint64_t seed) {  \
+        if (n < 0 || !(eb > 0) || (kind != 0 && kind != 1)) return PMSZO_ERR_ARG;               \
+        const T eps = (T)eb;                                                                     \
+        const double step = 2.0 * eb;                                                            \
+        const uint64_t salt = (seed & 0xFFFFFFFFull) << 40;                                      \
+        _Pragma("omp parallel for schedule(static)")                                             \
+        for (int64_t i = 0; i < n; ++i) {                                                        \
+            const T fv = f[i];                                                                   \
+            T v;                                                                                 \
+            if (kind == 0) {                                                                     \
+                v = (T)(step * rint((double)fv / step));                                         \
+            } else {                                                                             \
+                const uint64_t h = pmszo_splitmix64((uint64_t)i ^ salt);                         \
+                const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;    \
+                v = (T)((double)fv + eb * u);                                                    \
+            }                                                                                    \
+            if (!(FABS(fv - v) <= eps)) v = fv;                                                  \
+            fh[i] = v;                                                                           \
+        }                                                                                        \
+        return PMSZO_OK;                                                                         \
+    }
+
+PMSZO_DEFINE_STANDIN(float, f32, fabsf)
+PMSZO_DEFINE_STANDIN(double, f64, fabs)

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -759,23 +760,15 @@ static_assert(kOffReq % 256 == 0 && kOffSlots % 256 == 0, "sub-arrays stay 256-b
 // codes | edit counters | request bitmap | two active bitmaps | sweep slots
 static __device__ __align__(256) unsigned char g_scratch[kBytes];
 
-// Host-side address of g_scratch per device, looked up once per device with
-// that device current (the host symbol itself is not a device address).
-constexpr int kMaxDevices = 64;
-static std::mutex g_mu;
-static unsigned char *g_addr[kMaxDevices] = {};
-
+// Device address of g_scratch in the calling thread's current context.  The
+// host-side symbol is only a stand-in for the array, so the address is looked
+// up with cudaGetSymbolAddress (which allocates nothing) on every call: a
+// cached address would go stale after cudaDeviceReset or in another context
+// on the same device, where the library's device code is loaded again.
 static int scratch_address(unsigned char **out) {
-    int dev = 0;
-    PMSZ_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return set_error(PMSZ_ERR_ARG, "device ordinal beyond the supported range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        PMSZ_CUDA(cudaGetSymbolAddress(&p, g_scratch));
-        g_addr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_addr[dev];
+    void *p = nullptr;
+    PMSZ_CUDA(cudaGetSymbolAddress(&p, g_scratch));
+    *out = static_cast<unsigned char *>(p);
     return PMSZ_OK;
 }
 
@@ -815,6 +808,11 @@ int run(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pms
     PMSZ_CUDA(cudaMemsetAsync(act[0], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(act[1], 0, g.nwords * 4, s));
     PMSZ_CUDA(cudaMemsetAsync(slots, 0, sizeof(SweepSlot) * static_cast<size_t>(max_sweeps), s));
+    // ms_total: host clock from here to the last sweep's read-back; the loop
+    // synchronises the stream after every sweep, so this is the device window
+    // of the loop (timing events are not created: they are driver resources)
+    PMSZ_CUDA(cudaStreamSynchronize(s));
+    const auto t0 = std::chrono::steady_clock::now();
 
     const T eps = static_cast<T>(eb);
     const T delta = static_cast<T>(eb / static_cast<double>(q));
@@ -859,7 +857,8 @@ int run(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pms
         res->sweeps = sweeps;
         res->iteration = sweeps + 1;
         res->edits = edits;
-        res->ms_first_pass = res->ms_detect = res->ms_apply = res->ms_total = 0.0;
+        res->ms_first_pass = res->ms_detect = res->ms_apply = 0.0;
+        res->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         res->launches = 2 * sweeps;
     }
     return status;

@@ -297,3 +297,37 @@ def test_plateau_field_matches_oracle(cuda, dtype):
     assert int(r.log[1, 6]) > (1 << 16)  # sweep 2 runs as a list sweep
     np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
     np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+def test_c1_plain_64cubed_f32_sz3_matches_oracle(cuda):
+    """The CPU-runnable workload exactly as stated: 64^3 fp32 Perlin fBm (seed
+    0, 4 octaves, base frequency 1/32, persistence 0.5, lacunarity 2,
+    normalised to [0,1]), SZ-like stand-in at eps = 1e-3.  Field, sweep
+    count, per-sweep counters and the printed iteration equal the oracle's."""
+    shape, eb = (64, 64, 64), 1e-3
+    f = F.perlin_field(shape, 0, 4, 1 / 32, 0.5, 2.0, dtype=np.float32)
+    fh = F.standin(f, eb, "sz3", 0)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    dfh = _dev(fh, cuda)
+    r = api().correct(_dev(f, cuda), dfh, eb)
+    assert r.status == st == capi.PMSZ_OK
+    assert r.sweeps == sw and r.iteration == sw + 1
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+def test_c2_plain_512cubed_f64_zfp_matches_oracle(cuda):
+    """The headline workload at full size: 512^3 fp64 Perlin fBm (seed 1, 5
+    octaves, base frequency 1/64, persistence 0.5), ZFP-like stand-in at
+    eps = 1e-4, bit for bit against the oracle (about 10 s of CPU on 16
+    cores)."""
+    shape, eb = (512, 512, 512), 1e-4
+    df = api().gen_perlin(shape, 1, 5, 1 / 64, 0.5, 2.0, dtype=torch.float64)
+    dfh = api().standin(df, eb, "zfp", 1)
+    f, fh = df.cpu().numpy(), dfh.cpu().numpy()
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    r = api().correct(df, dfh, eb)
+    assert r.status == st == capi.PMSZ_OK
+    assert r.sweeps == sw
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint64), ref.view(np.uint64))
+    np.testing.assert_array_equal(r.log[:, :5], recs)

@@ -279,3 +279,31 @@ def test_naive_is_thread_count_independent():
         O.set_threads(n0)
     assert a[0].tobytes() == b[0].tobytes()
     np.testing.assert_array_equal(a[4], b[4])
+
+
+# ------------------------------------------------ host-core field generator
+
+@pytest.mark.parametrize("shape,seed,octaves,base,pers,dtype", [
+    ((24, 20, 36), 0, 4, 1 / 16, 0.5, np.float32),
+    ((33, 17, 40), 1, 5, 1 / 64, 0.5, np.float64),
+    ((16, 16, 16), 7, 6, 1 / 128, 0.55, np.float32),
+    ((64, 64, 64), 0, 4, 1 / 32, 0.5, np.float32),
+])
+def test_host_generator_matches_numpy(shape, seed, octaves, base, pers, dtype):
+    """The oracle's C generator (used by the benchmark's CPU legs so that they
+    load no GPU code) gives the numpy generator's bits, fields and stand-ins."""
+    a = F.perlin_field(shape, seed, octaves, base, pers, dtype=dtype)
+    b = O.perlin_field(shape, seed, octaves, base, pers, dtype=dtype)
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    for comp in ("sz3", "zfp"):
+        for eb in (1e-3, 1e-4, 3.7e-5):
+            x = F.standin(a, eb, comp, seed)
+            y = O.standin(a, eb, comp, seed)
+            assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), (comp, eb)
+
+
+def test_host_generator_rejects_bad_arguments():
+    with pytest.raises(ValueError):
+        O.standin(np.zeros((2, 2, 2), np.float32), 1e-3, "lz4")
+    with pytest.raises(ValueError):
+        O.standin(np.zeros((2, 2, 2), np.float32), -1.0, "zfp")

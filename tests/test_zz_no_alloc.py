@@ -34,6 +34,7 @@ def _noalloc(f, fh, eb, max_sweeps=4096):
                                 ctypes.byref(opts), ctypes.byref(res), torch.cuda.current_stream().cuda_stream)
     rows = np.array([[log[i].fmax, log[i].fmin, log[i].fdir, log[i].requested, log[i].changed]
                      for i in range(res.sweeps)], np.uint64)
+    _noalloc.ms_total = res.ms_total
     return st, res.sweeps, rows
 
 
@@ -61,6 +62,7 @@ def test_noalloc_matches_allocating_entry_point_twice(cuda, dtype, comp, shape, 
         torch.cuda.synchronize()
         assert st == st_ref
         assert sw == sw_ref
+        assert _noalloc.ms_total > 0.0      # the loop's window is measured
         assert torch.equal(out.view(torch.uint8), ref.view(torch.uint8))
         np.testing.assert_array_equal(log, log_ref)
 
