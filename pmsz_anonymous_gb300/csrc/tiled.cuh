@@ -153,7 +153,9 @@ __host__ __device__ constexpr int tile_slot_sel(int r) { return rank_dz(r) + 1; 
 //            appended to xlist (k_first_exact decides it on full keys), so no
 //            warp runs a one-lane exact path inside the plane loop and no
 //            full keys are staged.
-template <typename T, int MODE, bool DEFER = false>
+//   INT      the block's tile, its halo and the planes zb-1 .. ze lie inside
+//            the domain: no bound checks, every voxel has its 15 cells.
+template <typename T, int MODE, bool DEFER = false, bool INT = false>
 __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *__restrict__ fa,
                                            const T *__restrict__ fb, uint8_t *__restrict__ codes,
                                            uint32_t *__restrict__ hp, uint32_t *__restrict__ req,
@@ -181,7 +183,7 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
         const int cy = c / kHX, cx = c - cy * kHX;
         const int gx = x0 - 1 + cx, gy = y0 - 1 + cy;
         cell_s[j] = c;
-        cell_in[j] = c < kCells && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+        cell_in[j] = c < kCells && (INT || (gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny));
         cell_own[j] = cell_in[j] && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY;
         cell_g[j] = cell_in[j] ? static_cast<size_t>(gx) + static_cast<size_t>(gy) * g.nx : 0;
     }
@@ -194,7 +196,7 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
     // fp64 pass runs five blocks per SM to hold them without spills: 1.98
     // against 2.08 ms at 512^3); fp32 passes stash at once (measured faster).
     auto fetch_plane = [&](int zz, T (&v)[2][NF]) {
-        const bool zin = zz >= 0 && zz < g.nz;
+        const bool zin = INT || (zz >= 0 && zz < g.nz);
         const size_t zoff = zin ? static_cast<size_t>(zz) * plane : 0;
 #pragma unroll
         for (int j = 0; j < 2; ++j)
@@ -204,7 +206,7 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
     };
     auto stash_plane = [&](int zz, const T (&v)[2][NF]) {
         const int s = zz & (kRing - 1);
-        const bool zin = zz >= 0 && zz < g.nz;
+        const bool zin = INT || (zz >= 0 && zz < g.nz);
         const bool zown = zz >= zb && zz < ze;
         const size_t zoff = zin ? static_cast<size_t>(zz) * plane : 0;
 #pragma unroll
@@ -264,8 +266,8 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
         if (zz <= ze) load_plane(zz);
     __syncthreads();
     uint32_t cmax = 0, cmin = 0, cdir = 0, active = 0;
-    const bool in = x < g.nx && y < g.ny;
-    const bool xy_interior = x0 >= 1 && x0 + kTX <= g.nx - 1 && y >= 1 && y <= g.ny - 2;  // warp-uniform
+    const bool in = INT || (x < g.nx && y < g.ny);
+    const bool xy_interior = INT || (x0 >= 1 && x0 + kTX <= g.nx - 1 && y >= 1 && y <= g.ny - 2);  // warp-uniform
     constexpr bool kOverlap = sizeof(T) == 8;
     for (int z0 = zb; z0 < ze; z0 += kPer) {
         T pend[kPer][2][NF];  // the planes this iteration prefetches, stashed after its compute
@@ -278,7 +280,7 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
 #pragma unroll 1
         for (int z = z0; z < min(z0 + kPer, ze); ++z) {
             const int slots[3] = {(z + kRing - 1) & (kRing - 1), z & (kRing - 1), (z + 1) & (kRing - 1)};
-            const bool interior = xy_interior && z >= 1 && z <= g.nz - 2;
+            const bool interior = INT || (xy_interior && z >= 1 && z <= g.nz - 2);
             uint32_t tm = 0;
             if (in) {
                 const size_t i = flat(g, x, y, z);
@@ -289,7 +291,57 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
                     int oasc, odesc;
                     Ext e;
                     bool decided = true;
-                    if (MODE == kFirst) {
+                    if constexpr (MODE == kFirst && DEFER && INT) {
+                        // Interior voxels of the deferring first pass: the four
+                        // chains of f, then of fhat (15 proxies live at a time);
+                        // a chain pair certifies its winner when the two ranks
+                        // sum to 15, so one test covers all four certificates;
+                        // the rules run only where the two codes differ (equal
+                        // codes fire no rule unless the voxel is both maximum
+                        // and minimum of f, code 0x77).
+                        uint32_t M0, m0, N0, n0, M1, m1, N1, n1;
+                        {
+                            uint32_t ta[15];
+#pragma unroll
+                            for (int r = 0; r < 15; ++r)
+                                ta[r] = sm.p[0][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+                            M0 = ta[0]; m0 = ta[0]; N0 = ta[0] + 15u; n0 = N0;
+#pragma unroll
+                            for (int r = 1; r < 15; ++r) {
+                                const uint32_t a = ta[r] + static_cast<uint32_t>(r), b = ta[r] + static_cast<uint32_t>(15 - r);
+                                M0 = max(M0, a); m0 = min(m0, a); N0 = max(N0, b); n0 = min(n0, b);
+                            }
+                        }
+                        {
+                            uint32_t tb[15];
+#pragma unroll
+                            for (int r = 0; r < 15; ++r)
+                                tb[r] = sm.p[1][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+                            M1 = tb[0]; m1 = tb[0]; N1 = tb[0] + 15u; n1 = N1;
+#pragma unroll
+                            for (int r = 1; r < 15; ++r) {
+                                const uint32_t a = tb[r] + static_cast<uint32_t>(r), b = tb[r] + static_cast<uint32_t>(15 - r);
+                                M1 = max(M1, a); m1 = min(m1, a); N1 = max(N1, b); n1 = min(n1, b);
+                            }
+                        }
+                        const uint32_t s0 = (M0 + N0) & (m0 + n0);
+                        const uint32_t c0 = (M0 & 15u) | ((m0 & 15u) << 4), c1 = (M1 & 15u) | ((m1 & 15u) << 4);
+                        decided = false;
+                        if ((s0 & (M1 + N1) & (m1 + n1) & 15u) != 15u) {
+                            codes[i] = (s0 & 15u) == 15u ? static_cast<uint8_t>(c0) : kCodeUnset;
+                            const uint32_t pos = atomicAdd(&sm.xn, 1u);
+                            if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
+                            else spill_append(xlist, xcount, static_cast<uint32_t>(i));
+                        } else {
+                            codes[i] = static_cast<uint8_t>(c0);
+                            if (c1 != c0 || c0 == 0x77u) {
+                                tm = detect_rules(static_cast<int>(c1 & 15u), static_cast<int>(c1 >> 4),
+                                                  static_cast<int>(c0 & 15u), static_cast<int>(c0 >> 4), cmax, cmin,
+                                                  cdir);
+                                if (tm) request_targets(req, g, x, y, z, tm);
+                            }
+                        }
+                    } else if (MODE == kFirst) {
                         const Ext o = ext(0, z, slots, interior);
                         oasc = o.asc;
                         odesc = o.desc;
@@ -322,7 +374,7 @@ __device__ __forceinline__ void tiled_body(TileOf<T, MODE, DEFER> &sm, const T *
             }
             if (MODE != kCodes) {
                 const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
-                if (tx == 0 && y < g.ny && mism) act_next[word_of(g, x0, y, z)] = mism;
+                if (tx == 0 && (INT || y < g.ny) && mism) act_next[word_of(g, x0, y, z)] = mism;
             }
         }
         // their ring slots were last read kPer iterations ago (not by this one)
@@ -353,8 +405,18 @@ __global__ void __launch_bounds__(kThreads, MODE == kFirst && DEFER && sizeof(T)
                                                        SweepSlot *slot, Geom g, int bz0, uint32_t *xlist = nullptr,
                                                        uint32_t *xcount = nullptr) {
     __shared__ TileOf<T, MODE, DEFER> sm;
-    tiled_body<T, MODE, DEFER>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y,
-                               bz0 + static_cast<int>(blockIdx.z), xlist, xcount);
+    const int bz = bz0 + static_cast<int>(blockIdx.z);
+    // a block whose tile, halo included, and planes zb-1 .. ze lie inside the
+    // domain runs the check-free body (about three blocks in four at 512^3)
+    const int x0 = static_cast<int>(blockIdx.x) * kTX, y0 = static_cast<int>(blockIdx.y) * kTY, zb = bz * g.zc;
+    const bool inside = x0 >= 1 && x0 + kTX + 1 <= g.nx && y0 >= 1 && y0 + kTY + 1 <= g.ny && zb >= 1 &&
+                        zb + g.zc + 1 <= g.nz;
+    if (inside)
+        tiled_body<T, MODE, DEFER, true>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
+                                         xlist, xcount);
+    else
+        tiled_body<T, MODE, DEFER, false>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
+                                          xlist, xcount);
 }
 
 // ---------------------------------------------------------------------------
