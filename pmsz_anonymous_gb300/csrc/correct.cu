@@ -23,6 +23,8 @@
 #include "helpers.cuh"
 #include "internal.h"
 
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
 #include <algorithm>
 #include <cstring>
 #include <chrono>
@@ -197,6 +199,68 @@ static inline unsigned stride_grid(size_t items) {
     return static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(want, 152 * 16)));
 }
 
+// Tensor maps of f and fhat for the TMA-fed first pass (k_first_tma): 3-D
+// (nx, ny, nz) maps with a box of one tile plane.  The encoder is the driver's
+// cuTensorMapEncodeTiled, reached through the runtime (the library does not
+// link libcuda).  Not available (ok = false: the first pass loads its tiles
+// itself) when the encoder is missing, the fields are not 16-byte aligned or
+// a row is not a multiple of 16 bytes.
+struct FirstMaps {
+    CUtensorMap f, fh;
+    bool ok = false;
+};
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+template <typename T>
+static FirstMaps first_maps(const T *f, const T *fh, const Geom &g) {
+    FirstMaps m;
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || (static_cast<size_t>(g.nx) * sizeof(T)) % 16 || reinterpret_cast<uintptr_t>(f) % 16 ||
+        reinterpret_cast<uintptr_t>(fh) % 16)
+        return m;
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(g.nx), static_cast<cuuint64_t>(g.ny),
+                                static_cast<cuuint64_t>(g.nz)};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(g.nx) * sizeof(T),
+                                   static_cast<cuuint64_t>(g.nx) * g.ny * sizeof(T)};
+    const cuuint32_t box[3] = {static_cast<cuuint32_t>(RawBox<T>::kX), static_cast<cuuint32_t>(kHY), 1u};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    const CUtensorMapDataType dt = sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    for (int k = 0; k < 2; ++k)
+        if (enc(k ? &m.fh : &m.f, dt, 3, const_cast<T *>(k ? fh : f), dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return m;
+    m.ok = true;
+    return m;
+}
+
+// The deferring first pass over the z-chunks bz0 .. bz0+grid.z-1: TMA-fed
+// interior blocks when the maps exist; *err is set if a plane's copy did not
+// arrive within the bounded wait.
+template <typename T>
+static void launch_first_pass(const FirstMaps &m, dim3 grid, cudaStream_t s, const T *f, T *fh, uint8_t *codes,
+                              uint32_t *hp, uint32_t *req, uint32_t *act, SweepSlot *slot, const Geom &g, int bz0,
+                              uint32_t *xl, uint32_t *xc, uint32_t *err) {
+    const dim3 blk(kTX, kTY, 1);
+    if (m.ok)
+        k_first_tma<T><<<grid, blk, 0, s>>>(m.f, m.fh, f, fh, codes, hp, req, act, slot, g, bz0, xl, xc, err);
+    else
+        k_tiled<T, kFirst, true><<<grid, blk, 0, s>>>(f, fh, codes, hp, req, act, slot, g, bz0, xl, xc);
+}
+
 // Runs sweeps first.. in one cooperative launch of k_tail_loop (grid = the
 // number of co-resident blocks) after summarising the active bitmap of sweep
 // `first`; *done receives the total number of sweeps.
@@ -268,7 +332,7 @@ int check_geom(size_t nx, size_t ny, size_t nz) {
 template <typename T>
 int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
                       uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches,
-                      uint32_t *xlist, uint32_t *xcount) {
+                      uint32_t *xlist, uint32_t *xcount, const FirstMaps *maps = nullptr, uint32_t *err = nullptr) {
     if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
     const int nchunks = (g.nz + g.zc - 1) / g.zc;
@@ -315,8 +379,7 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
         dim3 grid = tiled_grid(g);
         grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
         if (xlist)  // deferring first pass (see k_first_exact)
-            k_tiled<T, kFirst, true><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps, xlist,
-                                                            xcount);
+            launch_first_pass<T>(*maps, grid, s, f, fh, codes, hp, req, a_next, slot, g, j * cps, xlist, xcount, err);
         else
             k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
         PMSZ_CUDA(cudaGetLastError());
@@ -374,6 +437,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     LoopState *ls = use_list ? ws.at<LoopState>(o_ls) : nullptr;
     const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
     const unsigned list_blocks = 152 * 8;
+    const FirstMaps maps = use_list ? first_maps<T>(f, fh, g) : FirstMaps{};
     EventTimer et;
     if ((rc = et.init())) return rc;
     PMSZ_CUDA(cudaEventRecord(et.ev[3], s));  // start of the loop's device window
@@ -420,11 +484,11 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         if (ingest) {
             if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches, xlist,
-                                           &ls->lc[3])))
+                                           &ls->lc[3], &maps, &ls->err)))
                 return rc;
         } else {
-            k_tiled<T, kFirst, true><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act[1], &ls->cur, g, 0,
-                                                                     xlist, &ls->lc[3]);
+            launch_first_pass<T>(maps, tiled_grid(g), s, f, fh, codes, hp, req, act[1], &ls->cur, g, 0, xlist,
+                                 &ls->lc[3], &ls->err);
             ++launches;
         }
         k_first_exact<T><<<list_blocks, 256, 0, s>>>(xlist, &ls->lc[3], f, fh, codes, req, act[1], &ls->cur, g,
@@ -485,6 +549,8 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         if (!hls) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
         PMSZ_CUDA(cudaMemcpyAsync(hls, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
         PMSZ_CUDA(cudaStreamSynchronize(s));
+        if (hls->err)
+            return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
         const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
         const int64_t nloop = std::max<int64_t>(done - 1, 0);
         launches += 16 * std::max<int64_t>(1, (nloop + 1) / 2);
@@ -655,12 +721,14 @@ int time_first_pass(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, ui
     Workspace ws(s);
     const size_t o_hp = ws.reserve<uint32_t>(g.n), o_req = ws.reserve<uint32_t>(g.nwords),
                  o_act = ws.reserve<uint32_t>(g.nwords), o_slot = ws.reserve<SweepSlot>(1),
-                 o_x = ws.reserve<uint32_t>(defer ? g.n : 0), o_xc = ws.reserve<uint32_t>(1);
+                 o_x = ws.reserve<uint32_t>(defer ? g.n : 0), o_xc = ws.reserve<uint32_t>(2);
     int rc = ws.commit();
     if (rc) return rc;
+    const FirstMaps maps = defer ? first_maps<T>(f, fh, g) : FirstMaps{};
     uint32_t *hp = ws.at<uint32_t>(o_hp), *req = ws.at<uint32_t>(o_req), *act = ws.at<uint32_t>(o_act);
-    uint32_t *xl = ws.at<uint32_t>(o_x), *xc = ws.at<uint32_t>(o_xc);
+    uint32_t *xl = ws.at<uint32_t>(o_x), *xc = ws.at<uint32_t>(o_xc), *err = xc + 1;
     SweepSlot *slot = ws.at<SweepSlot>(o_slot);
+    PMSZ_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
     EventTimer et;
     if ((rc = et.init())) return rc;
     const dim3 blk3(kTX, kTY, 1);
@@ -674,7 +742,8 @@ int time_first_pass(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, ui
             PMSZ_CUDA(cudaMemsetAsync(xc, 0, sizeof(uint32_t), s));
             PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
             if (defer)
-                k_tiled<T, kFirst, true><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act, slot, g, 0, xl, xc);
+                launch_first_pass<T>(maps, tiled_grid(g), s, f, const_cast<T *>(fh), codes, hp, req, act, slot, g, 0, xl,
+                                     xc, err);
             else
                 k_tiled<T, kFirst><<<tiled_grid(g), blk3, 0, s>>>(f, fh, codes, hp, req, act, slot, g, 0);
             PMSZ_CUDA(cudaGetLastError());
@@ -685,6 +754,13 @@ int time_first_pass(const T *f, const T *fh, size_t nx, size_t ny, size_t nz, ui
             if (rep > 0 && (best == 0.f || t < best)) best = t;
         }
         ms[k] = best;
+    }
+    if (defer) {
+        uint32_t herr = 0;
+        PMSZ_CUDA(cudaMemcpyAsync(&herr, err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        if (herr)
+            return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
     }
     if (defer) {  // the deferred voxels' code bytes: codes is complete for the caller
         k_first_exact<T><<<152 * 8, 256, 0, s>>>(xl, xc, f, fh, codes, req, act, slot, g, g.div_nx);

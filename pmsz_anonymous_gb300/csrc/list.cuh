@@ -435,6 +435,7 @@ struct LoopState {
     int go;
     int exact_keys;  // fp32 list detection on exact keys (k_pick_detection)
     uint32_t lc[4];  // active list, request list, exact list
+    uint32_t err;    // set by the first pass when a tensor copy did not arrive
     SweepSlot cur;
 };
 

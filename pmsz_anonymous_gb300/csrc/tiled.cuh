@@ -23,6 +23,7 @@
 // boundary branch is needed on the fast path.
 #pragma once
 #include <cooperative_groups.h>
+#include <cuda.h>  // CUtensorMap (the map itself is encoded on the host)
 
 #include "helpers.cuh"
 
@@ -417,6 +418,220 @@ __global__ void __launch_bounds__(kThreads, MODE == kFirst && DEFER && sizeof(T)
     else
         tiled_body<T, MODE, DEFER, false>(sm, fa, fb, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
                                           xlist, xcount);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-fed first pass.  A block whose tile, halo and planes zb-1 .. ze lie
+// inside the domain gets its planes by tensor-map copies: one thread issues,
+// per plane, a cp.async.bulk.tensor box of f and one of fhat (the tile with
+// its one-voxel halo, widened in x so that the box starts on a 16-byte
+// boundary) into a ring of kRawStages shared-memory stages, each guarded by an
+// mbarrier that the copy engine completes with the box's byte count.  The
+// threads wait for a plane, convert each of its cells to a proxy once (the
+// same conversion, proxy write and NaN / sentinel check as the load path of
+// tiled_body), and the stage is refilled with the plane kRawStages ahead
+// after the barrier that ends the plane.  No thread computes a global address
+// or predicates a load for the tile; the compute is tiled_body's interior
+// deferring path.  Blocks on the domain's faces run tiled_body.
+//
+// Every mbarrier wait is bounded: a plane that does not arrive within the
+// limit sets *err (the host reports PMSZ_ERR_CUDA), and the block still waits,
+// again bounded, on every plane it issued before it exits.
+// ---------------------------------------------------------------------------
+template <typename T> struct RawBox;
+template <> struct RawBox<double> { static constexpr int kX = 36, kOff = 1; };  // x0-2 .. x0+33
+template <> struct RawBox<float> { static constexpr int kX = 40, kOff = 3; };   // x0-4 .. x0+35
+constexpr int kRawStages = 4;
+template <typename T>
+constexpr int kRawBytes = RawBox<T>::kX * kHY * static_cast<int>(sizeof(T));  // one box of one field
+template <typename T>
+constexpr int kRawPitch = (kRawBytes<T> + 127) / 128 * 128;  // stages start on 128-byte boundaries
+
+template <typename T>
+struct __align__(128) TmaTile {
+    unsigned char raw[kRawStages][2][kRawPitch<T>];  // boxes of f and fhat, x fastest, rows of RawBox<T>::kX
+    uint32_t p[2][4][kHY][kHX];                      // proxy ring, as tiled_body's
+    uint32_t x[kFirstXCap];                          // voxels whose certificate failed
+    unsigned long long mbar[kRawStages];
+    uint32_t xn, xbase;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+constexpr int kMbarTries = 1 << 22;  // try_wait suspends between tries: a bound of seconds, not a spin count
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (int it = 0; it < kMbarTries; ++it) {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(ok) : "r"(addr), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t mbar) {
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(mbar) : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap *tf, const CUtensorMap *tfh,
+                                               uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
+                                               uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                               SweepSlot *slot, const Geom &g, int bx, int by, int bz,
+                                               uint32_t *__restrict__ xlist, uint32_t *xcount, uint32_t *err) {
+    constexpr int kBX = RawBox<T>::kX, kOff = RawBox<T>::kOff;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
+    const int x0 = bx * kTX, y0 = by * kTY, zb = bz * g.zc, ze = zb + g.zc;  // inside: ze <= nz - 1
+    const int x = x0 + tx, y = y0 + ty;
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+    const int nplanes = g.zc + 2;  // zb-1 .. ze
+    if (tid == 0) {
+        for (int s = 0; s < kRawStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&sm.mbar[s])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sm.xn = 0;
+    }
+    __syncthreads();
+    auto issue = [&](int k) {  // plane zb-1+k into stage k % kRawStages
+        const int s = k % kRawStages;
+        const uint32_t mb = smem_u32(&sm.mbar[s]);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage's reads come first
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mb), "r"(2 * kRawBytes<T>)
+                     : "memory");
+        tma_load_3d(smem_u32(sm.raw[s][0]), tf, x0 - kOff - 1, y0 - 1, zb - 1 + k, mb);
+        tma_load_3d(smem_u32(sm.raw[s][1]), tfh, x0 - kOff - 1, y0 - 1, zb - 1 + k, mb);
+    };
+    if (tid == 0)
+        for (int k = 0; k < kRawStages && k < nplanes; ++k) issue(k);
+
+    // this thread's cells (tid and tid + 256 of the 34 x 10 halo tile)
+    int cell_s[2], cell_r[2];
+    bool cell_own[2];
+    size_t cell_g[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int c = tid + j * kThreads;
+        const int cy = c / kHX, cx = c - cy * kHX;
+        cell_s[j] = c;
+        cell_r[j] = cy * kBX + cx + kOff;
+        cell_own[j] = c < kCells && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY;
+        cell_g[j] = static_cast<size_t>(x0 - 1 + cx) + static_cast<size_t>(y0 - 1 + cy) * g.nx;
+    }
+    uint32_t bad = 0, failed = 0;
+    auto convert = [&](int k) {  // stage of plane zb-1+k -> its proxy slot
+        const int s = k % kRawStages, zz = zb - 1 + k;
+        if (!mbar_wait(smem_u32(&sm.mbar[s]), static_cast<uint32_t>((k / kRawStages) & 1))) failed = 1;
+        const bool zown = zz >= zb && zz < ze;
+        const int ps = zz & 3;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (cell_s[j] >= kCells) continue;
+#pragma unroll
+            for (int F = 0; F < 2; ++F) {
+                const T v = reinterpret_cast<const T *>(sm.raw[s][F])[cell_r[j]];
+                const uint32_t px = proxy_of(v);
+                if (cell_own[j] && zown) {
+                    bad |= bad_value(v) ? 1u : 0u;
+                    if (F == 1) hp[static_cast<size_t>(zz) * plane + cell_g[j]] = px;
+                }
+                (&sm.p[F][ps][0][0])[cell_s[j]] = px;
+            }
+        }
+    };
+    convert(0);
+    convert(1);
+    convert(2);
+    __syncthreads();
+    if (tid == 0)
+        for (int k = kRawStages; k < kRawStages + 3 && k < nplanes; ++k) issue(k);  // stages of planes 0..2
+    uint32_t cmax = 0, cmin = 0, cdir = 0;
+    size_t i = static_cast<size_t>(x) + static_cast<size_t>(y) * g.nx + static_cast<size_t>(zb) * plane;
+    for (int z = zb; z < ze; ++z, i += plane) {
+        const int slots[3] = {(z + 3) & 3, z & 3, (z + 1) & 3};
+        uint32_t tm = 0;
+        uint32_t M0, m0, N0, n0, M1, m1, N1, n1;  // the four chains of f, then of fhat
+        {
+            uint32_t ta[15];
+#pragma unroll
+            for (int r = 0; r < 15; ++r) ta[r] = sm.p[0][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+            M0 = ta[0]; m0 = ta[0]; N0 = ta[0] + 15u; n0 = N0;
+#pragma unroll
+            for (int r = 1; r < 15; ++r) {
+                const uint32_t a = ta[r] + static_cast<uint32_t>(r), b = ta[r] + static_cast<uint32_t>(15 - r);
+                M0 = max(M0, a); m0 = min(m0, a); N0 = max(N0, b); n0 = min(n0, b);
+            }
+        }
+        {
+            uint32_t tb[15];
+#pragma unroll
+            for (int r = 0; r < 15; ++r) tb[r] = sm.p[1][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+            M1 = tb[0]; m1 = tb[0]; N1 = tb[0] + 15u; n1 = N1;
+#pragma unroll
+            for (int r = 1; r < 15; ++r) {
+                const uint32_t a = tb[r] + static_cast<uint32_t>(r), b = tb[r] + static_cast<uint32_t>(15 - r);
+                M1 = max(M1, a); m1 = min(m1, a); N1 = max(N1, b); n1 = min(n1, b);
+            }
+        }
+        const uint32_t s0 = (M0 + N0) & (m0 + n0);
+        const uint32_t c0 = (M0 & 15u) | ((m0 & 15u) << 4), c1 = (M1 & 15u) | ((m1 & 15u) << 4);
+        if ((s0 & (M1 + N1) & (m1 + n1) & 15u) != 15u) {
+            codes[i] = (s0 & 15u) == 15u ? static_cast<uint8_t>(c0) : kCodeUnset;
+            const uint32_t pos = atomicAdd(&sm.xn, 1u);
+            if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
+            else spill_append(xlist, xcount, static_cast<uint32_t>(i));
+        } else {
+            codes[i] = static_cast<uint8_t>(c0);
+            if (c1 != c0 || c0 == 0x77u) {
+                tm = detect_rules(static_cast<int>(c1 & 15u), static_cast<int>(c1 >> 4), static_cast<int>(c0 & 15u),
+                                  static_cast<int>(c0 >> 4), cmax, cmin, cdir);
+                if (tm) request_targets(req, g, x, y, z, tm);
+            }
+        }
+        const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
+        if (tx == 0 && mism) act_next[word_of(g, x0, y, z)] = mism;
+        const int k = z - zb + 3;  // plane z+2
+        if (k < nplanes) convert(k);
+        __syncthreads();
+        if (tid == 0 && k + kRawStages < nplanes) issue(k + kRawStages);
+    }
+    if (failed) atomicOr(err, 1u);
+    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, static_cast<uint32_t>(ze - zb), bad};
+    block_flush_slot(slot, v);
+    const uint32_t nb = min(sm.xn, kFirstXCap);
+    if (tid == 0) sm.xbase = nb ? atomicAdd(xcount, nb) : 0u;
+    __syncthreads();
+    for (uint32_t j = tid; j < nb; j += kThreads) xlist[sm.xbase + j] = sm.x[j];
+}
+
+// The deferring first pass with TMA-fed interior blocks (tiled_body on the
+// domain's faces); tf / tfh map f / fhat as (nx, ny, nz) with a box of
+// RawBox<T>::kX x 10 x 1.  bz0 as for k_tiled.
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 5) k_first_tma(const __grid_constant__ CUtensorMap tf,
+                                                            const __grid_constant__ CUtensorMap tfh,
+                                                            const T *__restrict__ f, const T *__restrict__ fh,
+                                                            uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
+                                                            uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
+                                                            SweepSlot *slot, Geom g, int bz0, uint32_t *xlist,
+                                                            uint32_t *xcount, uint32_t *err) {
+    __shared__ union Tile {
+        TmaTile<T> t;
+        TileOf<T, kFirst, true> s;
+    } sm;
+    const int bz = bz0 + static_cast<int>(blockIdx.z);
+    const int x0 = static_cast<int>(blockIdx.x) * kTX, y0 = static_cast<int>(blockIdx.y) * kTY, zb = bz * g.zc;
+    const bool inside = x0 >= 1 && x0 + kTX + 1 <= g.nx && y0 >= 1 && y0 + kTY + 1 <= g.ny && zb >= 1 &&
+                        zb + g.zc + 1 <= g.nz;
+    if (inside)
+        first_tma_body<T>(sm.t, &tf, &tfh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz, xlist, xcount,
+                          err);
+    else
+        tiled_body<T, kFirst, true, false>(sm.s, f, fh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
+                                           xlist, xcount);
 }
 
 // ---------------------------------------------------------------------------
