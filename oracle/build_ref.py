@@ -11,6 +11,9 @@
   same way.
 * ``oracle/_ref/ref_harness`` -- ``oracle/ref_harness.cpp`` (driver API),
   compiled on the machine that runs it.
+* ``oracle/_ref/ref_encoder`` -- ``oracle/ref_encoder.cu``: the unmodified
+  ``pMSz.cu`` included whole, host side, with the real ``libzstd.so.1``; it
+  runs the reference's own edit-file encoder on the host (no GPU needed).
 
 Everything lands in ``oracle/_ref/`` (git-ignored).
 """
@@ -31,6 +34,7 @@ CUBIN = os.path.join(OUT, "pmsz_ref.cubin")
 NAIVE_SRC = os.path.join(REF_DIR, "naive_MSz.cu")
 NAIVE_CUBIN = os.path.join(OUT, "naive_ref.cubin")
 HARNESS = os.path.join(OUT, "ref_harness")
+ENCODER = os.path.join(OUT, "ref_encoder")
 
 
 def _cuda_home() -> str:
@@ -69,7 +73,25 @@ def build_harness() -> str:
     return HARNESS
 
 
+def build_encoder() -> str | None:
+    """pMSz.cu (host side) + oracle/ref_encoder.cu -> ref_encoder; None where
+    the reference's sources are absent."""
+    src = os.path.join(HERE, "ref_encoder.cu")
+    if not os.path.exists(REF_SRC):
+        return ENCODER if os.path.exists(ENCODER) else None
+    os.makedirs(OUT, exist_ok=True)
+    deps = [src, REF_SRC, os.path.join(HERE, "ref_shim", "zstd.h")]
+    if not os.path.exists(ENCODER) or any(os.path.getmtime(ENCODER) < os.path.getmtime(d) for d in deps):
+        cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-std=c++17", "-O1", "-gencode",
+               "arch=compute_103a,code=sm_103a", "-I" + os.path.join(HERE, "ref_shim"), "-I" + REF_DIR, src, "-o",
+               ENCODER, "-l:libzstd.so.1", "-Xcompiler", "-w"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return ENCODER
+
+
 if __name__ == "__main__":
     print(build_cubin())
     if "--harness" in sys.argv:
         print(build_harness())
+    if "--encoder" in sys.argv:
+        print(build_encoder())

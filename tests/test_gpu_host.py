@@ -160,3 +160,36 @@ def test_cli_reconstruct_rebuilds_the_corrected_field(cuda, tmp_path):
     p = subprocess.run([exe, "--reconstruct", f"{decp},{nx},{ny},{nz}", repr(eb), "--out", str(rec), "--deltas",
                         str(tmp_path / "missing.bin")], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert p.returncode != 0
+
+
+@pytest.mark.parametrize("name", ["sz3", "zfp"])
+def test_cli_edit_files_match_the_reference_encoder(cuda, tmp_path, name):
+    """The CLI on the fields whose edit output the reference's own kernels
+    produced (tests/golden/extract_perlin_*.npz): its _deltas.bin and
+    _edits.bin carry the payloads that the reference's own encoder made of
+    that output (tests/golden/encoder_cases.npz), byte for byte when this
+    machine's libzstd is the one that made them."""
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    g = np.load(os.path.join(here, "golden", f"extract_perlin_{name}.npz"))
+    cases = np.load(os.path.join(here, "golden", "encoder_cases.npz"))
+    k = next(i for i in range(int(cases["n_delta"])) if str(cases[f"d{i}_name"]) == f"reference_extract_{name}")
+    c = next(i for i in range(int(cases["n_clamp"])) if str(cases[f"c{i}_name"]) == f"reference_extract_{name}")
+    exe = _cli()
+    f, fh, eb = g["f"], g["fh"], float(g["eb"])
+    path, decp = tmp_path / "field.bin", tmp_path / "decp.bin"
+    f.tofile(path)
+    fh.tofile(decp)
+    nz, ny, nx = f.shape
+    p = subprocess.run([exe, f"{path},{nx},{ny},{nz}", repr(eb), name, "1", "1", "1", "--decp", str(decp)],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    A = api()
+    blob_d = (tmp_path / "_deltas.bin").read_bytes()
+    blob_e = (tmp_path / "_edits.bin").read_bytes()
+    ref_d, ref_e = cases[f"d{k}_out"].tobytes(), cases[f"c{c}_out"].tobytes()
+    np.testing.assert_array_equal(A.decode_deltas(blob_d, f.size), A.decode_deltas(ref_d, f.size))
+    np.testing.assert_array_equal(A.decode_clamps(blob_e, np.float64).view(np.uint8),
+                                  A.decode_clamps(ref_e, np.float64).view(np.uint8))
+    if A.zstd_version() == int(cases["zstd_version"]):
+        assert blob_d == ref_d and blob_e == ref_e
