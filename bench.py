@@ -76,13 +76,17 @@ def parse(argv=None):
                    help="z-slices of the CPU sample (0 = the whole field: about 10 s on 16 cores at 512^3 fp64)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5)
-    p.add_argument("--workload", choices=["plain", "batch", "serve", "reconstruct"], default="plain",
+    p.add_argument("--workload", choices=["plain", "batch", "serve", "reconstruct", "hostlink"], default="plain",
                    help="plain: one 512^3 field (the headline); batch: 64 mixed fp32 fields; "
                         "serve: Poisson job stream through the correction server; "
-                        "reconstruct: the decoder on the plain workload's field")
+                        "reconstruct: the decoder on the plain workload's field; "
+                        "hostlink: host<->device copy rates that bound the e2e number")
     p.add_argument("--serve-jobs", type=int, default=120)
     p.add_argument("--serve-rates", default="100,300,1000,3000", help="arrival rates (jobs/s) to sweep")
     p.add_argument("--batch-fields", type=int, default=64)
+    p.add_argument("--host-loop", action="store_true",
+                   help="enqueue the list sweeps from the host instead of the CUDA graph (for ncu, which does "
+                        "not profile kernels of graphs with conditional nodes)")
     p.add_argument("--no-extra", action="store_true",
                    help="plain workload only: skip the batch, serve and reference-kernel legs")
     return p.parse_args(argv)
@@ -292,14 +296,14 @@ def run_ours(args):
     tune = api.autotune(f, fh0) if not args.no_tune else None
     for _ in range(args.warmup):
         fh.copy_(fh0)
-        api.correct(f, fh, args.eb)
+        api.correct(f, fh, args.eb, host_loop=args.host_loop)
     barrier()
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
         for _ in range(args.steps):
             fh.copy_(fh0)
             start.record()
-            r = api.correct(f, fh, args.eb, timing=True)
+            r = api.correct(f, fh, args.eb, timing=True, host_loop=args.host_loop)
             stop.record()
             stop.synchronize()
             times.append(start.elapsed_time(stop))
@@ -317,11 +321,12 @@ def run_ours(args):
     # e2e through the host-buffer C ABI (pmsz_correct_host_*): pinned host f and
     # fhat copied in, correction, edit extraction, and the reference main's
     # host output -- the delta symbols and the clamp list -- copied back.
-    f_h = f.cpu().pin_memory()
-    fh_h = fh0.cpu().pin_memory()
-    deltas_h = torch.empty(api.packed_len(n), dtype=torch.uint8).pin_memory()
-    clamp_h = torch.empty(n, dtype=f.dtype).pin_memory()
     e2e_times, n_clamp, e2e_res = [], 0, None
+    if args.e2e_steps > 0:
+        f_h = f.cpu().pin_memory()
+        fh_h = fh0.cpu().pin_memory()
+        deltas_h = torch.empty(api.packed_len(n), dtype=torch.uint8).pin_memory()
+        clamp_h = torch.empty(n, dtype=f.dtype).pin_memory()
     for i in range(1 + args.e2e_steps if args.e2e_steps > 0 else 0):
         barrier()
         start.record()
@@ -587,6 +592,66 @@ def run_reconstruct(args):
         raise SystemExit("reconstruction differs from the corrected field")
 
 
+def run_hostlink(args):
+    """Host link rates for the plain workload's inputs: the H2D copy of f and
+    fhat (2 * N * sizeof(T) bytes, pinned and pageable host memory, one
+    stream and two) and the D2H copy of the packed delta symbols, each timed
+    with CUDA events over a 1 GiB buffer; reports the e2e floor the inputs'
+    copy sets."""
+    import torch
+    dev = torch.device("cuda", 0)
+    nx, ny, nz = (int(v) for v in args.shape.split(","))
+    item = 8 if args.dtype == "f64" else 4
+    nbytes = 1 << 30
+    pinned = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    pageable = torch.empty(nbytes, dtype=torch.uint8)
+    pageable.fill_(1)
+    pinned.fill_(1)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn, reps=5):
+        best = []
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            ev[0].record()
+            fn()
+            ev[1].record()
+            ev[1].synchronize()
+            if r:
+                best.append(ev[0].elapsed_time(ev[1]))
+        return nbytes / (statistics.median(best) * 1e-3) / 1e9
+
+    def two_streams(dst, src):
+        h = nbytes // 2
+        for k, st in enumerate((s1, s2)):
+            st.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(st):
+                dst[k * h:(k + 1) * h].copy_(src[k * h:(k + 1) * h], non_blocking=True)
+        torch.cuda.current_stream().wait_stream(s1)
+        torch.cuda.current_stream().wait_stream(s2)
+
+    rates = {
+        "h2d_pinned_gbs": timed(lambda: d.copy_(pinned, non_blocking=True)),
+        "h2d_pinned_two_streams_gbs": timed(lambda: two_streams(d, pinned)),
+        "h2d_pageable_gbs": timed(lambda: d.copy_(pageable), reps=3),
+        "d2h_pinned_gbs": timed(lambda: pinned.copy_(d, non_blocking=True)),
+        "d2h_pageable_gbs": timed(lambda: pageable.copy_(d), reps=3),
+    }
+    inputs = 2 * nx * ny * nz * item
+    numa = sorted(n for n in os.listdir("/sys/devices/system/node") if n.startswith("node")) \
+        if os.path.isdir("/sys/devices/system/node") else []
+    print(json.dumps({
+        "metric": "host link GB/s (1 GiB copies, CUDA events)", "value": rates["h2d_pinned_gbs"], "unit": "GB/s",
+        "n_gpus": 1, "higher_is_better": True, "data": "synthetic", "rates": rates,
+        "config": {"workload": f"host link for {nx}x{ny}x{nz} {args.dtype} inputs", "numa_nodes": numa,
+                   "host_cores": os.cpu_count()},
+        "e2e_floor_ms": inputs / (max(rates["h2d_pinned_gbs"], rates["h2d_pinned_two_streams_gbs"]) * 1e9) * 1e3,
+        "input_bytes": inputs,
+    }), flush=True)
+
+
 def serve_specs(count: int, base_seed: int = 1000):
     """Served stream: per-job seed base+id, 3-6 octaves, each axis log-uniform
     in 32..384, 70% fp32 / 30% fp64, eps log-uniform in [1e-5, 1e-2], sz3 /
@@ -698,6 +763,8 @@ def main():
         run_serve(args)
     elif args.workload == "reconstruct":
         run_reconstruct(args)
+    elif args.workload == "hostlink":
+        run_hostlink(args)
     else:
         run_ours(args)
 

@@ -58,6 +58,13 @@ extern "C" {
                                      first tuned on its own inputs
                                      (pmsz_autotune_*); without the flag the
                                      table is only read */
+#define PMSZ_FLAG_HOST_LOOP 64u   /* pmsz_correct_{f32,f64}: run the voxel-list
+                                     sweeps from the host, two per round trip
+                                     to the device-side stop rule, instead of
+                                     as a CUDA graph with a conditional while
+                                     node (same kernels, same results; for
+                                     profilers and debuggers that cannot
+                                     look into conditional graph nodes) */
 
 typedef struct pmsz_opts {
     int32_t q;           /* edit levels; the reference hard-codes q = 5 (pMSz.cu:2630) */

@@ -183,10 +183,10 @@ PMSZO_DEFINE_APPLY(double, f64, fabs)
 /*   R5 desc != odesc: fdir++; request odesc                               */
 /* Requests are recorded in req[] (byte per voxel).                        */
 /* ---------------------------------------------------------------------- */
-#define PMSZO_DEFINE_DETECT(T, SUF)                                            \
-    static void pmszo_detect_##SUF(const T *fh, int64_t nx, int64_t ny,        \
-                                   int64_t nz, const int64_t *oasc,            \
-                                   const int64_t *odesc, uint8_t *req,         \
+#define PMSZO_DEFINE_DETECT(T, SUF, IDX, ISUF)                                 \
+    static void pmszo_detect_##SUF##ISUF(const T *fh, int64_t nx, int64_t ny,  \
+                                   int64_t nz, const IDX *oasc,                \
+                                   const IDX *odesc, uint8_t *req,             \
                                    pmszo_sweep_t *out) {                       \
         uint64_t cmax = 0, cmin = 0, cdir = 0;                                 \
         _Pragma("omp parallel for schedule(static) reduction(+:cmax,cmin,cdir)") \
@@ -197,8 +197,8 @@ PMSZO_DEFINE_APPLY(double, f64, fabs)
                     int64_t asc, desc;                                         \
                     pmszo_steepest_##SUF(fh, nx, ny, nz, x, y, z, &asc, &desc); \
                     const int is_max = asc == i, is_min = desc == i;           \
-                    const int omax = oasc[i] == i;                             \
-                    const int omin = !omax && odesc[i] == i;                   \
+                    const int omax = (int64_t)oasc[i] == i;                    \
+                    const int omin = !omax && (int64_t)odesc[i] == i;          \
                     const int r1 = is_max != omax, r2 = is_min != omin;        \
                     if (r1) {                                                  \
                         ++cmax;                                                \
@@ -207,18 +207,18 @@ PMSZO_DEFINE_APPLY(double, f64, fabs)
                     }                                                          \
                     if (r2) {                                                  \
                         ++cmin;                                                \
-                        int64_t t = omin ? i : odesc[i];                       \
+                        int64_t t = omin ? i : (int64_t)odesc[i];              \
                         _Pragma("omp atomic write") req[t] = 1;                \
                     }                                                          \
                     if (r1 || r2) {                                            \
                         ++cdir;                                                \
                         continue;                                              \
                     }                                                          \
-                    if (asc != oasc[i]) {                                      \
+                    if (asc != (int64_t)oasc[i]) {                             \
                         ++cdir;                                                \
                         _Pragma("omp atomic write") req[asc] = 1;              \
                     }                                                          \
-                    if (desc != odesc[i]) {                                    \
+                    if (desc != (int64_t)odesc[i]) {                           \
                         ++cdir;                                                \
                         _Pragma("omp atomic write") req[odesc[i]] = 1;         \
                     }                                                          \
@@ -228,8 +228,30 @@ PMSZO_DEFINE_APPLY(double, f64, fabs)
         out->fdir = cdir;                                                      \
     }
 
-PMSZO_DEFINE_DETECT(float, f32)
-PMSZO_DEFINE_DETECT(double, f64)
+PMSZO_DEFINE_DETECT(float, f32, int64_t, _i64)
+PMSZO_DEFINE_DETECT(double, f64, int64_t, _i64)
+PMSZO_DEFINE_DETECT(float, f32, uint32_t, _u32)
+PMSZO_DEFINE_DETECT(double, f64, uint32_t, _u32)
+
+/* Labelling into 32-bit indices (fields of fewer than 2^32 voxels: the same
+ * values in half the memory, so the oracle reaches 1536^3 on one host). */
+#define PMSZO_DEFINE_LABEL32(T, SUF)                                           \
+    static void pmszo_label32_##SUF(const T *v, int64_t nx, int64_t ny,        \
+                                    int64_t nz, uint32_t *asc, uint32_t *desc) { \
+        _Pragma("omp parallel for schedule(static)")                           \
+        for (int64_t z = 0; z < nz; ++z)                                       \
+            for (int64_t y = 0; y < ny; ++y)                                   \
+                for (int64_t x = 0; x < nx; ++x) {                             \
+                    const int64_t i = x + nx * (y + ny * z);                   \
+                    int64_t a, d;                                              \
+                    pmszo_steepest_##SUF(v, nx, ny, nz, x, y, z, &a, &d);      \
+                    asc[i] = (uint32_t)a;                                      \
+                    desc[i] = (uint32_t)d;                                     \
+                }                                                              \
+    }
+
+PMSZO_DEFINE_LABEL32(float, f32)
+PMSZO_DEFINE_LABEL32(double, f64)
 
 /* ---------------------------------------------------------------------- */
 /* The correction loop, c_loops at one rank (pMSz.cu:1872-2074):          */
@@ -255,8 +277,10 @@ PMSZO_DEFINE_DETECT(double, f64)
         const int64_t n = nx * ny * nz;                                        \
         const T eps = (T)eb;                                                   \
         const T delta = (T)(eb / (double)q);                                   \
-        int64_t *oasc = (int64_t *)malloc((size_t)n * sizeof(int64_t));        \
-        int64_t *odesc = (int64_t *)malloc((size_t)n * sizeof(int64_t));       \
+        const int narrow = n <= (int64_t)UINT32_MAX;                           \
+        const size_t isz = narrow ? sizeof(uint32_t) : sizeof(int64_t);        \
+        void *oasc = malloc((size_t)n * isz);                                  \
+        void *odesc = malloc((size_t)n * isz);                                 \
         uint8_t *req = (uint8_t *)calloc((size_t)n, 1);                        \
         uint8_t *cnt = cnt_out ? cnt_out : (uint8_t *)malloc((size_t)n);       \
         if (!oasc || !odesc || !req || !cnt) {                                 \
@@ -265,13 +289,21 @@ PMSZO_DEFINE_DETECT(double, f64)
             return PMSZO_ERR_OOM;                                              \
         }                                                                      \
         memset(cnt, 0, (size_t)n);                                             \
-        pmszo_label_##SUF(f, nx, ny, nz, oasc, odesc);                         \
+        if (narrow)                                                            \
+            pmszo_label32_##SUF(f, nx, ny, nz, (uint32_t *)oasc, (uint32_t *)odesc); \
+        else                                                                   \
+            pmszo_label_##SUF(f, nx, ny, nz, (int64_t *)oasc, (int64_t *)odesc); \
         int status = PMSZO_ERR_NOT_CONVERGED;                                  \
         int64_t sweeps = 0, edits = 0;                                         \
         while (sweeps < max_sweeps) {                                          \
             pmszo_sweep_t s;                                                   \
             memset(&s, 0, sizeof(s));                                          \
-            pmszo_detect_##SUF(fh, nx, ny, nz, oasc, odesc, req, &s);          \
+            if (narrow)                                                        \
+                pmszo_detect_##SUF##_u32(fh, nx, ny, nz, (const uint32_t *)oasc,   \
+                                         (const uint32_t *)odesc, req, &s);        \
+            else                                                               \
+                pmszo_detect_##SUF##_i64(fh, nx, ny, nz, (const int64_t *)oasc,    \
+                                         (const int64_t *)odesc, req, &s);         \
             ++sweeps;                                                          \
             uint64_t requested = 0, changed = 0, progressed = 0;               \
             _Pragma("omp parallel for schedule(static) reduction(+:requested,changed,progressed)") \

@@ -85,12 +85,14 @@ def _log_rows(log, k: int, first: int = 0) -> np.ndarray:
 
 def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_sweeps: int = 10000,
             full_sweeps: bool = False, timing: bool = False, stream=None, strategy: str = "pmsz",
-            autotune: bool = False) -> CorrectResult:
+            autotune: bool = False, host_loop: bool = False) -> CorrectResult:
     """Correct fhat in place so that its extrema and both segmentations match f
     (c_loops, pMSz.cu:1872-2074).  strategy="naive" runs the naive-MSz loop
     instead (naive_MSz.cu:1887-2220; full_sweeps and timing do not apply).
     autotune=True tunes the field's shape class on these inputs first when the
-    tuning table has no entry for it (PMSZ_FLAG_AUTOTUNE).
+    tuning table has no entry for it (PMSZ_FLAG_AUTOTUNE).  host_loop=True
+    enqueues the list sweeps from the host instead of a CUDA graph
+    (PMSZ_FLAG_HOST_LOOP; same results).
     Raises PmszError except for PMSZ_ERR_NOT_CONVERGED, which is reported in
     the result."""
     _check_field(f, "f")
@@ -99,7 +101,7 @@ def correct(f: torch.Tensor, fhat: torch.Tensor, eb: float, q: int = 5, max_swee
         raise ValueError("f and fhat must share shape, dtype and device")
     L = capi.load()
     flags = ((capi.PMSZ_FLAG_FULL_SWEEPS if full_sweeps else 0) | (capi.PMSZ_FLAG_TIMING if timing else 0) |
-             (capi.PMSZ_FLAG_AUTOTUNE if autotune else 0))
+             (capi.PMSZ_FLAG_AUTOTUNE if autotune else 0) | (capi.PMSZ_FLAG_HOST_LOOP if host_loop else 0))
     opts = capi.Opts(int(q), flags, int(max_sweeps))
     log = _sweep_log(int(max_sweeps))
     res = capi.Result(0, 0, 0, ctypes.cast(log, ctypes.POINTER(capi.SweepRecord)), int(max_sweeps))

@@ -22,6 +22,7 @@ PMSZ_FLAG_EDITS_ONLY = 4
 PMSZ_FLAG_NAIVE = 8
 PMSZ_FLAG_AUTOTUNE = 16
 PMSZ_FLAG_PACKED_DELTAS = 32
+PMSZ_FLAG_HOST_LOOP = 64
 
 
 class Opts(ctypes.Structure):

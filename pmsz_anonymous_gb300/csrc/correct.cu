@@ -504,45 +504,69 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         PMSZ_CUDA(cudaGetLastError());
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
 
-        struct GraphGuard {
-            cudaGraph_t graph = nullptr;
-            cudaGraphExec_t exec = nullptr;
-            cudaStream_t cs = nullptr;
-            ~GraphGuard() {
-                if (exec) cudaGraphExecDestroy(exec);
-                if (graph) cudaGraphDestroy(graph);
-                if (cs) cudaStreamDestroy(cs);
+        // One body: two list sweeps (odd: act[1] -> act[0], even: act[0] ->
+        // act[1]), each ending with k_loop_gate; with set_cond the second gate
+        // also sets the graph's while condition.
+        auto enqueue_body = [&](cudaStream_t bs, cudaGraphConditionalHandle cond, bool set_cond) {
+            for (int half = 0; half < 2; ++half) {
+                uint32_t *a_cur = act[half == 0 ? 1 : 0], *a_next = act[half == 0 ? 0 : 1];
+                compact_bitmap(a_cur, g, bcnt, list, &ls->lc[0], &ls->go, bs);
+                k_detect_list<T><<<list_blocks, 256, 0, bs>>>(list, &ls->lc[0], fh, hp, codes, req, a_next, xlist,
+                                                              &ls->lc[2], &ls->cur, g, div_nx, &ls->go,
+                                                              &ls->exact_keys, &ls->deferred);
+                k_detect_exact<T><<<list_blocks, 256, 0, bs>>>(xlist, &ls->lc[2], fh, codes, req, a_next, &ls->cur, g,
+                                                               div_nx, &ls->go);
+                compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, bs);
+                k_apply_list<T><<<list_blocks, 256, 0, bs>>>(list, &ls->lc[1], f, fh, cnt, hp, a_next, &ls->cur, g,
+                                                             div_nx, eps, delta, q, &ls->go);
+                k_loop_gate<<<1, 32, 0, bs>>>(ls, slots, max_sweeps, tail_at, cond, set_cond && half == 1 ? 1 : 0);
             }
-        } gg;
-        PMSZ_CUDA(cudaGraphCreate(&gg.graph, 0));
-        cudaGraphConditionalHandle cond;
-        PMSZ_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.graph, 1, cudaGraphCondAssignDefault));
-        cudaGraphNodeParams cp = {};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = cond;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        cudaGraphNode_t wnode;
-        PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, nullptr, nullptr, 0, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        PMSZ_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
-        PMSZ_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-        for (int half = 0; half < 2; ++half) {
-            uint32_t *a_cur = act[half == 0 ? 1 : 0], *a_next = act[half == 0 ? 0 : 1];
-            compact_bitmap(a_cur, g, bcnt, list, &ls->lc[0], &ls->go, gg.cs);
-            k_detect_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[0], fh, hp, codes, req, a_next, xlist,
-                                                             &ls->lc[2], &ls->cur, g, div_nx, &ls->go,
-                                                             &ls->exact_keys);
-            k_detect_exact<T><<<list_blocks, 256, 0, gg.cs>>>(xlist, &ls->lc[2], fh, codes, req, a_next, &ls->cur, g,
-                                                              div_nx, &ls->go);
-            compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, gg.cs);
-            k_apply_list<T><<<list_blocks, 256, 0, gg.cs>>>(list, &ls->lc[1], f, fh, cnt, hp, a_next, &ls->cur, g,
-                                                            div_nx, eps, delta, q, &ls->go);
-            k_loop_gate<<<1, 32, 0, gg.cs>>>(ls, slots, max_sweeps, tail_at, cond, half);
+        };
+        int64_t bodies = 0;
+        if (flags & PMSZ_FLAG_HOST_LOOP) {
+            // the same sweeps enqueued from the host, two per round trip to the
+            // device gate (tools that cannot look into conditional graph nodes)
+            int *hgo = static_cast<int *>(host_pinned(sizeof(int)));
+            if (!hgo) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+            for (;;) {
+                PMSZ_CUDA(cudaMemcpyAsync(hgo, &ls->go, sizeof(int), cudaMemcpyDeviceToHost, s));
+                PMSZ_CUDA(cudaStreamSynchronize(s));
+                if (!*hgo) break;
+                enqueue_body(s, cudaGraphConditionalHandle{}, false);
+                PMSZ_CUDA(cudaGetLastError());
+                ++bodies;
+            }
+        } else {
+            // The graph: one conditional while node whose body is enqueue_body,
+            // captured while sweep 0 runs; no host round trip between sweeps.
+            struct GraphGuard {
+                cudaGraph_t graph = nullptr;
+                cudaGraphExec_t exec = nullptr;
+                cudaStream_t cs = nullptr;
+                ~GraphGuard() {
+                    if (exec) cudaGraphExecDestroy(exec);
+                    if (graph) cudaGraphDestroy(graph);
+                    if (cs) cudaStreamDestroy(cs);
+                }
+            } gg;
+            PMSZ_CUDA(cudaGraphCreate(&gg.graph, 0));
+            cudaGraphConditionalHandle cond;
+            PMSZ_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.graph, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = cond;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t wnode;
+            PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, nullptr, nullptr, 0, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            PMSZ_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
+            PMSZ_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            enqueue_body(gg.cs, cond, true);
+            PMSZ_CUDA(cudaStreamEndCapture(gg.cs, &body));
+            PMSZ_CUDA(cudaGraphInstantiate(&gg.exec, gg.graph, 0));
+            PMSZ_CUDA(cudaGraphLaunch(gg.exec, s));
         }
-        PMSZ_CUDA(cudaStreamEndCapture(gg.cs, &body));
-        PMSZ_CUDA(cudaGraphInstantiate(&gg.exec, gg.graph, 0));
-        PMSZ_CUDA(cudaGraphLaunch(gg.exec, s));
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[3], s));
 
         LoopState *hls = static_cast<LoopState *>(host_pinned(sizeof(LoopState)));
@@ -553,7 +577,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
         const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
         const int64_t nloop = std::max<int64_t>(done - 1, 0);
-        launches += 16 * std::max<int64_t>(1, (nloop + 1) / 2);
+        launches += 16 * ((flags & PMSZ_FLAG_HOST_LOOP) ? bodies : std::max<int64_t>(1, (nloop + 1) / 2));
         if (timing) {  // the list sweeps' edits run inside the graph and count as detection time
             float a = 0, b = 0, c = 0;
             PMSZ_CUDA(cudaEventElapsedTime(&a, lt.ev[0], lt.ev[1]));

@@ -10,8 +10,9 @@
 //                   (requests and marks are bit ORs, counters sums)
 //   k_detect_list   one thread per listed voxel: the 15 proxies, the rules,
 //                   the requests, the mismatch bit of the next active set;
-//                   failed certificates go to a second list
-//   k_detect_exact  the second list on full keys
+//                   failed certificates are decided on full keys by the
+//                   block after its list loop (a full buffer spills)
+//   k_detect_exact  the spilled ones, on full keys
 //   compaction      request bitmap -> list
 //   k_apply_list    one thread per requested voxel: the edit, the proxy
 //                   refresh, the closed-stencil marks of the next active set
@@ -71,14 +72,17 @@ static __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint
 // gives the entry of bit 0 of the thread's word j (a word's entries are base
 // + bit), lane_ex is the thread's exclusive prefix of bit counts within its
 // warp and wbase its warp's offset in the step.  Block-uniform choice:
-//  - the step fits the 32 KB staging buffer: every thread writes its own
+//  - the step fits the staging buffer: every thread writes its own
 //    entries into shared memory at their ranks, then the block copies the
 //    step out with coalesced stores;
 //  - denser steps: the words and their bases are staged per warp and the
 //    warp visits its non-zero words in order, every lane writing the entry of
 //    its own bit of the word at the bit's rank, so each word's entries go out
 //    as one contiguous store and no thread loops over more than its bit.
-constexpr uint32_t kStageBytes = 32768;
+// 24 KB: nine compaction blocks fit on an SM, so the 8-per-SM grid runs in one
+// wave (32 KB allowed seven: 1.14 waves, 7 % slower at 512^3); a step of the
+// first list sweeps (about 5000 entries) still fits.
+constexpr uint32_t kStageBytes = 24576;
 template <typename E, class Base>
 __device__ __forceinline__ void write_step_entries(const uint32_t (&w)[4], uint32_t lane_ex, uint32_t wbase,
                                                    uint32_t step, unsigned char *raw, E *out, Base &&base) {
@@ -224,8 +228,10 @@ __device__ __forceinline__ void detect_outcome(const Geom &g, int x, int y, int 
 
 // Detection of every listed voxel (iscriticle data_type=0) on the proxy
 // array.  A voxel whose certificate fails (ties in the truncated proxies) is
-// appended to a second list and decided by k_detect_exact on full keys, so
-// this loop never runs a one-lane slow path.
+// buffered in shared memory and decided on full keys by the whole block after
+// its list loop, so the loop never runs a one-lane slow path; a full buffer
+// spills to a second list that k_detect_exact decides.  *deferred (or null)
+// counts the buffered and spilled voxels.
 constexpr uint32_t kExactCap = 2048;  // failed certificates buffered per block
 template <typename T>
 __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restrict__ list, const uint32_t *count,
@@ -234,9 +240,9 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
                                                      uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
                                                      uint32_t *__restrict__ exact_list, uint32_t *exact_count,
                                                      SweepSlot *slot, Geom g, FastDiv div_nx, const int *run,
-                                                     const int *exact_keys) {
+                                                     const int *exact_keys, uint32_t *deferred = nullptr) {
     __shared__ uint32_t s_exact[kExactCap];
-    __shared__ uint32_t s_n, s_base;
+    __shared__ uint32_t s_n;
     if (run && *run == 0) return;
     // fp32 with exact_keys set (k_pick_detection, k_loop_gate): the 4-byte keys
     // of fhat, gathered as the proxies would be, decide every voxel (no
@@ -284,12 +290,32 @@ __global__ void __launch_bounds__(256, 5) k_detect_list(const uint32_t *__restri
             else spill_append(exact_list, exact_count, i);
         }
     }
+    __syncthreads();  // s_n is final
+    const uint32_t nd = s_n, nb = min(nd, kExactCap);
+    if (deferred && threadIdx.x == 0 && nd) atomicAdd(deferred, nd);
+    // the buffered voxels on the 15 exact keys of fhat, one per thread; the
+    // keys are scanned one at a time (rank order, arg_ext's rule) so that this
+    // rare path adds no registers to the list loop
+    for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) {
+        const uint32_t i = s_exact[j];
+        int x, y, z;
+        voxel_coords(g, div_nx, i, x, y, z);
+        const uint32_t valid = valid_mask(x, y, z, g.nx, g.ny, g.nz);
+        using K = typename KeyOf<T>::type;
+        K bmax = 0, bmin = ~K(0);
+        int asc = kSelf, desc = kSelf;
+#pragma unroll 1
+        for (int r = 0; r < 15; ++r) {
+            if (!((valid >> r) & 1u)) continue;
+            const ptrdiff_t off = rank_dx(r) + rank_dy(r) * sy + rank_dz(r) * sz;
+            const K k = okey(__ldg(fh + (static_cast<ptrdiff_t>(i) + off)));
+            if (k >= bmax) { bmax = k; asc = r; }
+            if (k < bmin) { bmin = k; desc = r; }
+        }
+        detect_outcome(g, x, y, z, asc, desc, __ldg(codes + i), req, act_next, cmax, cmin, cdir);
+    }
     const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, active, 0u};
-    block_flush_slot(slot, v);  // ends with a barrier: s_n is final
-    const uint32_t nb = min(s_n, kExactCap);
-    if (threadIdx.x == 0) s_base = nb ? atomicAdd(exact_count, nb) : 0u;  // one global atomic per block
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) exact_list[s_base + j] = s_exact[j];
+    block_flush_slot(slot, v);
 }
 
 // The voxels whose certificate failed: steepest ranks on the 15 exact keys of
@@ -434,7 +460,8 @@ struct LoopState {
     long long k;
     int go;
     int exact_keys;  // fp32 list detection on exact keys (k_pick_detection)
-    uint32_t lc[4];  // active list, request list, exact list
+    uint32_t lc[4];  // active list, request list, exact list (spills), first-pass deferrals
+    uint32_t deferred;  // voxels of the current list sweep decided on exact keys
     uint32_t err;    // set by the first pass when a tensor copy did not arrive
     SweepSlot cur;
 };
@@ -469,7 +496,7 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
         slots[k] = c;
         // a list sweep that deferred more than a tenth of its voxels (failed
         // certificates) switches the following ones to exact keys, for good
-        if (10ull * ls->lc[2] > ls->lc[0]) ls->exact_keys = 1;
+        if (10ull * ls->deferred > ls->lc[0]) ls->exact_keys = 1;
         const bool stop = (k == 0 && c.bad) || (c.fmax == 0 && c.fmin == 0 && c.fdir == 0) || c.progressed == 0 ||
                           k + 1 >= max_sweeps;
         const bool tail = 15ull * c.changed + c.fdir <= tail_at;
@@ -477,6 +504,7 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
         ls->k = k + 1;
         ls->cur = SweepSlot{};
         ls->lc[0] = ls->lc[1] = ls->lc[2] = ls->lc[3] = 0;
+        ls->deferred = 0;
     }
     if (set_cond) cudaGraphSetConditional(cond, ls->go ? 1u : 0u);
 }

@@ -227,6 +227,12 @@ def test_large_field_through_the_device_sweep_loop(cuda, dtype, comp):
     rf = api().correct(df, full, eb, full_sweeps=True)
     assert rf.sweeps == sw
     assert torch.equal(full.view(torch.uint8), work.view(torch.uint8))
+    # the same list sweeps enqueued from the host instead of the graph
+    host = dfh.clone()
+    rh = api().correct(df, host, eb, host_loop=True)
+    assert rh.status == st and rh.sweeps == sw
+    assert torch.equal(host.view(torch.uint8), work.view(torch.uint8))
+    np.testing.assert_array_equal(rh.log[:, :5], recs)
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
