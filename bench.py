@@ -363,7 +363,7 @@ def run_ours(args):
                 "path": "pmsz_correct_host with PMSZ_FLAG_EDITS_ONLY | PMSZ_FLAG_PACKED_DELTAS: H2D f and fhat, "
                         "correction, edit extraction, D2H delta symbols packed at 3 bits (the reference's "
                         "pack_nbits) and the clamp list"},
-        "roofline": {"bound": "hbm", "kernel": "k_tiled<T,kFirst,DEFER> + k_first_exact (labelling + first detection)",
+        "roofline": {"bound": "hbm", "kernel": "k_first_tma + k_first_exact (labelling + first detection)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": bytes_first,
                      "ms_per_launch": statistics.mean(first_ms),
