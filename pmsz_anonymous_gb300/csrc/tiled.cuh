@@ -609,9 +609,11 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
 
 // The deferring first pass with TMA-fed interior blocks (tiled_body on the
 // domain's faces); tf / tfh map f / fhat as (nx, ny, nz) with a box of
-// RawBox<T>::kX x 10 x 1.  bz0 as for k_tiled.
+// RawBox<T>::kX x 10 x 1.  bz0 as for k_tiled.  fp32 runs six blocks per SM
+// (40 registers, no spills: 3.81 against 3.83 ms at 512^3); fp64 five (at
+// six it spills and is slower).
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 5) k_first_tma(const __grid_constant__ CUtensorMap tf,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 6 : 5) k_first_tma(const __grid_constant__ CUtensorMap tf,
                                                             const __grid_constant__ CUtensorMap tfh,
                                                             const T *__restrict__ f, const T *__restrict__ fh,
                                                             uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
