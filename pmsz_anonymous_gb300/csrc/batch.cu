@@ -41,8 +41,18 @@ __global__ void __launch_bounds__(kThreads, 5) k_first_multi(const Inst<T> *__re
     const uint32_t lt = blockIdx.x - __ldg(tpre + i);
     const uint32_t bx = lt % I.tiles_x, rest = lt / I.tiles_x;
     const uint32_t by = rest % I.tiles_y, bz = rest / I.tiles_y;
-    tiled_body<T, kFirst>(sm, I.f, I.fh, I.codes, I.hp, I.req, I.act1, I.slots, I.g, static_cast<int>(bx),
-                          static_cast<int>(by), static_cast<int>(bz));
+    // fp32 blocks whose tile, halo and planes zb-1 .. ze lie inside their
+    // field run the check-free body, as in k_tiled (21.8 against 21.97 ms on
+    // the 64-field batch; for fp64 the second body raises the spills)
+    const int x0 = static_cast<int>(bx) * kTX, y0 = static_cast<int>(by) * kTY, zb = static_cast<int>(bz) * I.g.zc;
+    const bool inside = x0 >= 1 && x0 + kTX + 1 <= I.g.nx && y0 >= 1 && y0 + kTY + 1 <= I.g.ny && zb >= 1 &&
+                        zb + I.g.zc + 1 <= I.g.nz;
+    if (sizeof(T) == 4 && inside)
+        tiled_body<T, kFirst, false, true>(sm, I.f, I.fh, I.codes, I.hp, I.req, I.act1, I.slots, I.g,
+                                           static_cast<int>(bx), static_cast<int>(by), static_cast<int>(bz));
+    else
+        tiled_body<T, kFirst>(sm, I.f, I.fh, I.codes, I.hp, I.req, I.act1, I.slots, I.g, static_cast<int>(bx),
+                              static_cast<int>(by), static_cast<int>(bz));
 }
 
 template <typename T>
