@@ -337,3 +337,43 @@ def test_c2_plain_512cubed_f64_zfp_matches_oracle(cuda):
     assert r.sweeps == sw
     np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint64), ref.view(np.uint64))
     np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+@pytest.mark.parametrize("shape,dtype", [
+    ((70, 66, 100), np.float64),   # rows of 800 bytes: TMA-fed interior blocks
+    ((70, 66, 99), np.float64),    # rows of 792 bytes (not a multiple of 16): threads load every tile
+    ((70, 66, 100), np.float32),   # rows of 400 bytes: TMA-fed interior blocks
+    ((70, 66, 98), np.float32),    # rows of 392 bytes: threads load every tile
+])
+def test_first_pass_tile_loaders_match_oracle(cuda, shape, dtype):
+    """Ragged fields large enough for interior blocks (tile, halo and planes
+    inside the domain), with and without the tensor-map tile loads, against
+    the oracle."""
+    eb = 1e-3
+    f, fh = _case(shape, dtype, "zfp", eb, 41, octaves=4, base=1 / 16)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    dfh = _dev(fh, cuda)
+    r = api().correct(_dev(f, cuda), dfh, eb)
+    assert r.status == st and r.sweeps == sw
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
+
+
+def test_first_pass_unaligned_fields_match_oracle(cuda):
+    """Fields that start 8 bytes past a 16-byte boundary (views into larger
+    buffers) cannot be described by tensor maps; the threads load the tiles and
+    the result is the oracle's."""
+    shape, eb = (66, 40, 96), 1e-3
+    f, fh = _case(shape, np.float64, "sz3", eb, 43, octaves=4, base=1 / 16)
+    ref, cnt, st, sw, recs = O.correct(f, fh, eb)
+    n = f.size
+    bf = torch.zeros(n + 1, dtype=torch.float64, device=cuda)
+    bh = torch.zeros(n + 1, dtype=torch.float64, device=cuda)
+    bf[1:] = torch.from_numpy(f.ravel()).to(cuda)
+    bh[1:] = torch.from_numpy(fh.ravel()).to(cuda)
+    df, dfh = bf[1:].view(shape), bh[1:].view(shape)
+    assert df.data_ptr() % 16 == 8
+    r = api().correct(df, dfh, eb)
+    assert r.status == st and r.sweeps == sw
+    np.testing.assert_array_equal(dfh.cpu().numpy().view(np.uint8), ref.view(np.uint8))
+    np.testing.assert_array_equal(r.log[:, :5], recs)
