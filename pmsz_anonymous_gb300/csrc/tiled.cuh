@@ -428,11 +428,13 @@ __global__ void __launch_bounds__(kThreads, MODE == kFirst && DEFER && sizeof(T)
 // boundary) into a ring of kRawStages shared-memory stages, each guarded by an
 // mbarrier that the copy engine completes with the box's byte count.  The
 // threads wait for a plane, convert each of its cells to a proxy once (the
-// same conversion, proxy write and NaN / sentinel check as the load path of
-// tiled_body), and the stage is refilled with the plane kRawStages ahead
-// after the barrier that ends the plane.  No thread computes a global address
-// or predicates a load for the tile; the compute is tiled_body's interior
-// deferring path.  Blocks on the domain's faces run tiled_body.
+// same conversion and NaN / sentinel check as the load path of tiled_body),
+// and the stage is refilled with the plane kRawStages ahead after the barrier
+// that ends the plane.  No thread computes a global address or predicates a
+// load for the tile; the compute is tiled_body's interior deferring path,
+// except that each voxel stores its own fhat proxy (coalesced) and that the
+// rules of voxels whose codes differ run after the last plane (kRuleCap).
+// Blocks on the domain's faces run tiled_body.
 //
 // Every mbarrier wait is bounded: a plane that does not arrive within the
 // limit sets *err (the host reports PMSZ_ERR_CUDA), and the block still waits,
@@ -442,6 +444,12 @@ template <typename T> struct RawBox;
 template <> struct RawBox<double> { static constexpr int kX = 36, kOff = 1; };  // x0-2 .. x0+33
 template <> struct RawBox<float> { static constexpr int kX = 40, kOff = 3; };   // x0-4 .. x0+35
 constexpr int kRawStages = 4;
+// Voxels of a TMA-fed block whose two codes differ are queued in shared
+// memory as (tx | ty << 5 | (z - zb) << 8 | c0 << 16 | c1 << 24) and run
+// through the rules by the whole block after its last plane: inline, a warp
+// would run the rules whenever one of its 32 voxels needs them.  A full queue
+// spills to the deferred list (k_first_exact decides those voxels on keys).
+constexpr uint32_t kRuleCap = 1024;
 template <typename T>
 constexpr int kRawBytes = RawBox<T>::kX * kHY * static_cast<int>(sizeof(T));  // one box of one field
 template <typename T>
@@ -452,8 +460,9 @@ struct __align__(128) TmaTile {
     unsigned char raw[kRawStages][2][kRawPitch<T>];  // boxes of f and fhat, x fastest, rows of RawBox<T>::kX
     uint32_t p[2][4][kHY][kHX];                      // proxy ring, as tiled_body's
     uint32_t x[kFirstXCap];                          // voxels whose certificate failed
+    uint32_t rq[kRuleCap];                           // voxels whose codes differ, for the rules (RuleEntry)
     unsigned long long mbar[kRawStages];
-    uint32_t xn, xbase;
+    uint32_t xn, xbase, rn;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -494,6 +503,7 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&sm.mbar[s])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         sm.xn = 0;
+        sm.rn = 0;
     }
     __syncthreads();
     auto issue = [&](int k) {  // plane zb-1+k into stage k % kRawStages
@@ -511,7 +521,6 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
     // this thread's cells (tid and tid + 256 of the 34 x 10 halo tile)
     int cell_s[2], cell_r[2];
     bool cell_own[2];
-    size_t cell_g[2];
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         const int c = tid + j * kThreads;
@@ -519,9 +528,11 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
         cell_s[j] = c;
         cell_r[j] = cy * kBX + cx + kOff;
         cell_own[j] = c < kCells && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY;
-        cell_g[j] = static_cast<size_t>(x0 - 1 + cx) + static_cast<size_t>(y0 - 1 + cy) * g.nx;
     }
     uint32_t bad = 0, failed = 0;
+    // fp64: only cells whose proxy lies in the ranges of the infinities and
+    // NaNs, or equals the proxy of the sentinel 1e30, take the exact test
+    const uint32_t sentinel_px = proxy_of(T(1e30));
     auto convert = [&](int k) {  // stage of plane zb-1+k -> its proxy slot
         const int s = k % kRawStages, zz = zb - 1 + k;
         if (!mbar_wait(smem_u32(&sm.mbar[s]), static_cast<uint32_t>((k / kRawStages) & 1))) failed = 1;
@@ -534,10 +545,9 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
             for (int F = 0; F < 2; ++F) {
                 const T v = reinterpret_cast<const T *>(sm.raw[s][F])[cell_r[j]];
                 const uint32_t px = proxy_of(v);
-                if (cell_own[j] && zown) {
+                if (cell_own[j] && zown &&
+                    (sizeof(T) == 4 || px - 0x00100000u >= 0xFFE00000u || px == sentinel_px))
                     bad |= bad_value(v) ? 1u : 0u;
-                    if (F == 1) hp[static_cast<size_t>(zz) * plane + cell_g[j]] = px;
-                }
                 (&sm.p[F][ps][0][0])[cell_s[j]] = px;
             }
         }
@@ -552,7 +562,7 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
     size_t i = static_cast<size_t>(x) + static_cast<size_t>(y) * g.nx + static_cast<size_t>(zb) * plane;
     for (int z = zb; z < ze; ++z, i += plane) {
         const int slots[3] = {(z + 3) & 3, z & 3, (z + 1) & 3};
-        uint32_t tm = 0;
+        bool rule = false;
         uint32_t M0, m0, N0, n0, M1, m1, N1, n1;  // the four chains of f, then of fhat
         {
             uint32_t ta[15];
@@ -569,6 +579,7 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
             uint32_t tb[15];
 #pragma unroll
             for (int r = 0; r < 15; ++r) tb[r] = sm.p[1][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+            hp[i] = tb[kSelf];  // the proxy array of fhat, one coalesced row per warp
             M1 = tb[0]; m1 = tb[0]; N1 = tb[0] + 15u; n1 = N1;
 #pragma unroll
             for (int r = 1; r < 15; ++r) {
@@ -585,18 +596,40 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
             else spill_append(xlist, xcount, static_cast<uint32_t>(i));
         } else {
             codes[i] = static_cast<uint8_t>(c0);
-            if (c1 != c0 || c0 == 0x77u) {
-                tm = detect_rules(static_cast<int>(c1 & 15u), static_cast<int>(c1 >> 4), static_cast<int>(c0 & 15u),
-                                  static_cast<int>(c0 >> 4), cmax, cmin, cdir);
-                if (tm) request_targets(req, g, x, y, z, tm);
+            rule = c1 != c0 || c0 == 0x77u;
+        }
+        const uint32_t want = __ballot_sync(0xFFFFFFFFu, rule);
+        if (want) {
+            uint32_t base = 0;
+            if (tx == 0) base = atomicAdd(&sm.rn, static_cast<uint32_t>(__popc(want)));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (rule) {
+                const uint32_t pos = base + static_cast<uint32_t>(__popc(want & ((1u << tx) - 1u)));
+                if (pos < kRuleCap && g.zc <= 256)
+                    sm.rq[pos] = static_cast<uint32_t>(tx) | (static_cast<uint32_t>(ty) << 5) |
+                                 (static_cast<uint32_t>(z - zb) << 8) | (c0 << 16) | (c1 << 24);
+                else
+                    spill_append(xlist, xcount, static_cast<uint32_t>(i));
             }
         }
-        const uint32_t mism = __ballot_sync(0xFFFFFFFFu, tm != 0);
-        if (tx == 0 && mism) act_next[word_of(g, x0, y, z)] = mism;
         const int k = z - zb + 3;  // plane z+2
         if (k < nplanes) convert(k);
         __syncthreads();
         if (tid == 0 && k + kRawStages < nplanes) issue(k + kRawStages);
+    }
+    // the queued rule voxels (every enqueue precedes the loop's last barrier)
+    const uint32_t nr = min(sm.rn, kRuleCap);
+    for (uint32_t j = tid; j < nr; j += kThreads) {
+        const uint32_t e = sm.rq[j];
+        const int ex = x0 + static_cast<int>(e & 31u), ey = y0 + static_cast<int>((e >> 5) & 7u),
+                  ez = zb + static_cast<int>((e >> 8) & 0xFFu);
+        const uint32_t c0 = (e >> 16) & 0xFFu, c1 = e >> 24;
+        const uint32_t tm = detect_rules(static_cast<int>(c1 & 15u), static_cast<int>(c1 >> 4),
+                                         static_cast<int>(c0 & 15u), static_cast<int>(c0 >> 4), cmax, cmin, cdir);
+        if (tm) {
+            request_targets(req, g, ex, ey, ez, tm);
+            atomicOr(act_next + word_of(g, x0, ey, ez), 1u << (e & 31u));
+        }
     }
     if (failed) atomicOr(err, 1u);
     const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, static_cast<uint32_t>(ze - zb), bad};
