@@ -486,7 +486,14 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
                  :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(mbar) : "memory");
 }
 
-template <typename T>
+// FACE: a block on a domain face (or one whose tile crosses the domain's far
+// end).  Planes outside the domain are not copied: their stage's barrier gets
+// a plain arrive and their cells proxy 0; cells of a box outside the domain
+// in x or y (the copy fills them with zeros) are stored as proxy 0 as well.
+// A warp whose row has a voxel on a face runs the general chains (proxy 0
+// loses every max chain as 0 + r and every min chain as 0 + r - 16, wrapped);
+// threads beyond the domain compute but store nothing.
+template <typename T, bool FACE>
 __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap *tf, const CUtensorMap *tfh,
                                                uint8_t *__restrict__ codes, uint32_t *__restrict__ hp,
                                                uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
@@ -494,10 +501,12 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
                                                uint32_t *__restrict__ xlist, uint32_t *xcount, uint32_t *err) {
     constexpr int kBX = RawBox<T>::kX, kOff = RawBox<T>::kOff;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
-    const int x0 = bx * kTX, y0 = by * kTY, zb = bz * g.zc, ze = zb + g.zc;  // inside: ze <= nz - 1
+    const int x0 = bx * kTX, y0 = by * kTY, zb = bz * g.zc;
+    const int ze = FACE ? min(g.nz, zb + g.zc) : zb + g.zc;  // inside: ze <= nz - 1
     const int x = x0 + tx, y = y0 + ty;
+    const bool vin = !FACE || (x < g.nx && y < g.ny);  // this thread's voxels exist
     const size_t plane = static_cast<size_t>(g.nx) * g.ny;
-    const int nplanes = g.zc + 2;  // zb-1 .. ze
+    const int nplanes = ze - zb + 2;  // zb-1 .. ze
     if (tid == 0) {
         for (int s = 0; s < kRawStages; ++s)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&sm.mbar[s])) : "memory");
@@ -509,6 +518,10 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
     auto issue = [&](int k) {  // plane zb-1+k into stage k % kRawStages
         const int s = k % kRawStages;
         const uint32_t mb = smem_u32(&sm.mbar[s]);
+        if (FACE && (zb - 1 + k < 0 || zb - 1 + k >= g.nz)) {  // nothing to copy: complete the phase
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(mb) : "memory");
+            return;
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage's reads come first
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mb), "r"(2 * kRawBytes<T>)
                      : "memory");
@@ -520,14 +533,16 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
 
     // this thread's cells (tid and tid + 256 of the 34 x 10 halo tile)
     int cell_s[2], cell_r[2];
-    bool cell_own[2];
+    bool cell_own[2], cell_in[2];
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         const int c = tid + j * kThreads;
         const int cy = c / kHX, cx = c - cy * kHX;
+        const int gx = x0 - 1 + cx, gy = y0 - 1 + cy;
         cell_s[j] = c;
         cell_r[j] = cy * kBX + cx + kOff;
-        cell_own[j] = c < kCells && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY;
+        cell_in[j] = !FACE || (gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny);
+        cell_own[j] = c < kCells && cx >= 1 && cx <= kTX && cy >= 1 && cy <= kTY && cell_in[j];
     }
     uint32_t bad = 0, failed = 0;
     // fp64: only cells whose proxy lies in the ranges of the infinities and
@@ -537,14 +552,15 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
         const int s = k % kRawStages, zz = zb - 1 + k;
         if (!mbar_wait(smem_u32(&sm.mbar[s]), static_cast<uint32_t>((k / kRawStages) & 1))) failed = 1;
         const bool zown = zz >= zb && zz < ze;
+        const bool zin = !FACE || (zz >= 0 && zz < g.nz);
         const int ps = zz & 3;
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             if (cell_s[j] >= kCells) continue;
 #pragma unroll
             for (int F = 0; F < 2; ++F) {
-                const T v = reinterpret_cast<const T *>(sm.raw[s][F])[cell_r[j]];
-                const uint32_t px = proxy_of(v);
+                const T v = zin ? reinterpret_cast<const T *>(sm.raw[s][F])[cell_r[j]] : T(0);
+                const uint32_t px = (!FACE || (zin && cell_in[j])) ? proxy_of(v) : 0u;
                 if (cell_own[j] && zown &&
                     (sizeof(T) == 4 || px - 0x00100000u >= 0xFFE00000u || px == sentinel_px))
                     bad |= bad_value(v) ? 1u : 0u;
@@ -560,36 +576,44 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
         for (int k = kRawStages; k < kRawStages + 3 && k < nplanes; ++k) issue(k);  // stages of planes 0..2
     uint32_t cmax = 0, cmin = 0, cdir = 0;
     size_t i = static_cast<size_t>(x) + static_cast<size_t>(y) * g.nx + static_cast<size_t>(zb) * plane;
+    // the four chains of one field (max / min, forward / reverse ranks); GEN:
+    // the general form, whose min chains add -16 so that proxy 0 loses
+    auto chains = [&](int F, const int (&slots)[3], bool gen, uint32_t &M, uint32_t &m, uint32_t &N, uint32_t &n,
+                      uint32_t &self) {
+        uint32_t t[15];
+#pragma unroll
+        for (int r = 0; r < 15; ++r) t[r] = sm.p[F][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
+        self = t[kSelf];
+        if (!FACE || !gen) {
+            M = t[0]; m = t[0]; N = t[0] + 15u; n = N;
+#pragma unroll
+            for (int r = 1; r < 15; ++r) {
+                const uint32_t a = t[r] + static_cast<uint32_t>(r), b = t[r] + static_cast<uint32_t>(15 - r);
+                M = max(M, a); m = min(m, a); N = max(N, b); n = min(n, b);
+            }
+        } else {
+            M = t[0]; m = t[0] - 16u; N = t[0] + 15u; n = t[0] - 1u;
+#pragma unroll
+            for (int r = 1; r < 15; ++r) {
+                const uint32_t a = t[r] + static_cast<uint32_t>(r), b = t[r] + static_cast<uint32_t>(15 - r);
+                M = max(M, a); m = min(m, a - 16u); N = max(N, b); n = min(n, b - 16u);
+            }
+        }
+    };
     for (int z = zb; z < ze; ++z, i += plane) {
         const int slots[3] = {(z + 3) & 3, z & 3, (z + 1) & 3};
+        // warp-uniform: every voxel of this warp's row has its 15 cells
+        const bool gen = FACE && !(y >= 1 && y + 1 < g.ny && z >= 1 && z + 1 < g.nz && x0 >= 1 && x0 + kTX + 1 <= g.nx);
         bool rule = false;
-        uint32_t M0, m0, N0, n0, M1, m1, N1, n1;  // the four chains of f, then of fhat
-        {
-            uint32_t ta[15];
-#pragma unroll
-            for (int r = 0; r < 15; ++r) ta[r] = sm.p[0][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
-            M0 = ta[0]; m0 = ta[0]; N0 = ta[0] + 15u; n0 = N0;
-#pragma unroll
-            for (int r = 1; r < 15; ++r) {
-                const uint32_t a = ta[r] + static_cast<uint32_t>(r), b = ta[r] + static_cast<uint32_t>(15 - r);
-                M0 = max(M0, a); m0 = min(m0, a); N0 = max(N0, b); n0 = min(n0, b);
-            }
-        }
-        {
-            uint32_t tb[15];
-#pragma unroll
-            for (int r = 0; r < 15; ++r) tb[r] = sm.p[1][slots[tile_slot_sel(r)]][ty + 1 + rank_dy(r)][tx + 1 + rank_dx(r)];
-            hp[i] = tb[kSelf];  // the proxy array of fhat, one coalesced row per warp
-            M1 = tb[0]; m1 = tb[0]; N1 = tb[0] + 15u; n1 = N1;
-#pragma unroll
-            for (int r = 1; r < 15; ++r) {
-                const uint32_t a = tb[r] + static_cast<uint32_t>(r), b = tb[r] + static_cast<uint32_t>(15 - r);
-                M1 = max(M1, a); m1 = min(m1, a); N1 = max(N1, b); n1 = min(n1, b);
-            }
-        }
+        uint32_t M0, m0, N0, n0, M1, m1, N1, n1, self0, self1;  // the four chains of f, then of fhat
+        chains(0, slots, gen, M0, m0, N0, n0, self0);
+        chains(1, slots, gen, M1, m1, N1, n1, self1);
+        (void)self0;
+        if (vin) hp[i] = self1;  // the proxy array of fhat, one coalesced row per warp
         const uint32_t s0 = (M0 + N0) & (m0 + n0);
         const uint32_t c0 = (M0 & 15u) | ((m0 & 15u) << 4), c1 = (M1 & 15u) | ((m1 & 15u) << 4);
-        if ((s0 & (M1 + N1) & (m1 + n1) & 15u) != 15u) {
+        if (!vin) {
+        } else if ((s0 & (M1 + N1) & (m1 + n1) & 15u) != 15u) {
             codes[i] = (s0 & 15u) == 15u ? static_cast<uint8_t>(c0) : kCodeUnset;
             const uint32_t pos = atomicAdd(&sm.xn, 1u);
             if (pos < kFirstXCap) sm.x[pos] = static_cast<uint32_t>(i);
@@ -632,7 +656,7 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
         }
     }
     if (failed) atomicOr(err, 1u);
-    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, static_cast<uint32_t>(ze - zb), bad};
+    const uint32_t v[8] = {cmax, cmin, cdir, 0u, 0u, 0u, vin ? static_cast<uint32_t>(ze - zb) : 0u, bad};
     block_flush_slot(slot, v);
     const uint32_t nb = min(sm.xn, kFirstXCap);
     if (tid == 0) sm.xbase = nb ? atomicAdd(xcount, nb) : 0u;
@@ -640,11 +664,13 @@ __device__ __forceinline__ void first_tma_body(TmaTile<T> &sm, const CUtensorMap
     for (uint32_t j = tid; j < nb; j += kThreads) xlist[sm.xbase + j] = sm.x[j];
 }
 
-// The deferring first pass with TMA-fed interior blocks (tiled_body on the
-// domain's faces); tf / tfh map f / fhat as (nx, ny, nz) with a box of
-// RawBox<T>::kX x 10 x 1.  bz0 as for k_tiled.  fp32 runs six blocks per SM
-// (40 registers, no spills: 3.81 against 3.83 ms at 512^3); fp64 five (at
-// six it spills and is slower).
+// The deferring first pass with TMA-fed tiles; tf / tfh map f / fhat as
+// (nx, ny, nz) with a box of RawBox<T>::kX x 10 x 1 (the caller falls back to
+// k_tiled where no map can be made: rows whose byte length is not a multiple
+// of 16, or base pointers off a 16-byte boundary).  f / fh are not read here.
+// bz0 as for k_tiled.  Interior blocks run the check-free body, blocks on a
+// face the FACE body.  fp32 runs six blocks per SM (40 registers, no spills:
+// 3.81 against 3.83 ms at 512^3); fp64 five (at six it spills and is slower).
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 6 : 5) k_first_tma(const __grid_constant__ CUtensorMap tf,
                                                             const __grid_constant__ CUtensorMap tfh,
@@ -653,20 +679,19 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 6 : 5) k_first_tma(
                                                             uint32_t *__restrict__ req, uint32_t *__restrict__ act_next,
                                                             SweepSlot *slot, Geom g, int bz0, uint32_t *xlist,
                                                             uint32_t *xcount, uint32_t *err) {
-    __shared__ union Tile {
-        TmaTile<T> t;
-        TileOf<T, kFirst, true> s;
-    } sm;
+    __shared__ TmaTile<T> sm;
+    (void)f;
+    (void)fh;
     const int bz = bz0 + static_cast<int>(blockIdx.z);
     const int x0 = static_cast<int>(blockIdx.x) * kTX, y0 = static_cast<int>(blockIdx.y) * kTY, zb = bz * g.zc;
     const bool inside = x0 >= 1 && x0 + kTX + 1 <= g.nx && y0 >= 1 && y0 + kTY + 1 <= g.ny && zb >= 1 &&
                         zb + g.zc + 1 <= g.nz;
     if (inside)
-        first_tma_body<T>(sm.t, &tf, &tfh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz, xlist, xcount,
-                          err);
+        first_tma_body<T, false>(sm, &tf, &tfh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
+                                 xlist, xcount, err);
     else
-        tiled_body<T, kFirst, true, false>(sm.s, f, fh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
-                                           xlist, xcount);
+        first_tma_body<T, true>(sm, &tf, &tfh, codes, hp, req, act_next, slot, g, blockIdx.x, blockIdx.y, bz,
+                                xlist, xcount, err);
 }
 
 // ---------------------------------------------------------------------------
