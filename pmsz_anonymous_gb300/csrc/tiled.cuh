@@ -457,13 +457,18 @@ constexpr int kRawPitch = (kRawBytes<T> + 127) / 128 * 128;  // stages start on 
 
 template <typename T>
 struct __align__(128) TmaTile {
-    unsigned char raw[kRawStages][2][kRawPitch<T>];  // boxes of f and fhat, x fastest, rows of RawBox<T>::kX
+    // first: the copy engine writes the stages, which must start on 128-byte
+    // boundaries (the struct is 128-byte aligned, kRawPitch a multiple of 128)
+    alignas(128) unsigned char raw[kRawStages][2][kRawPitch<T>];  // boxes of f and fhat, rows of RawBox<T>::kX
     uint32_t p[2][4][kHY][kHX];                      // proxy ring, as tiled_body's
     uint32_t x[kFirstXCap];                          // voxels whose certificate failed
     uint32_t rq[kRuleCap];                           // voxels whose codes differ, for the rules (RuleEntry)
     unsigned long long mbar[kRawStages];
     uint32_t xn, xbase, rn;
 };
+static_assert(offsetof(TmaTile<float>, raw) == 0 && offsetof(TmaTile<double>, raw) == 0 &&
+                  kRawPitch<float> % 128 == 0 && kRawPitch<double> % 128 == 0,
+              "TMA stages must start on 128-byte boundaries");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
