@@ -95,8 +95,9 @@ typedef struct pmsz_result {
     /* With PMSZ_FLAG_TIMING (else 0): device milliseconds of the fused
      * labelling + first detection pass, of all later detection passes, and of
      * all edit passes (sweeps that run inside the device-side sweep loop count
-     * whole, edits included, as detection time); launches = kernels launched
-     * by the call. */
+     * whole, edits included, as detection time; in the host-buffer calls,
+     * whose first sweeps run behind the copy in, the first-pass figure spans
+     * the copy and those sweeps); launches = kernels launched by the call. */
     double ms_first_pass, ms_detect, ms_apply;
     int64_t launches;
     /* Device milliseconds from the first to the last kernel of the loop

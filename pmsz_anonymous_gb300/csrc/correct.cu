@@ -389,6 +389,147 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
     return PMSZ_OK;
 }
 
+// Slabs of the host-buffer copy: whole z-chunks, about 64 MiB of f + fhat.
+struct IngestSlabs {
+    int cps, nchunks, nslabs;
+};
+static IngestSlabs ingest_slabs(const Geom &g, size_t elem) {
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+    const size_t chunk_bytes = 2 * plane * static_cast<size_t>(g.zc) * elem;
+    IngestSlabs r;
+    r.nchunks = (g.nz + g.zc - 1) / g.zc;
+    r.cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
+    r.nslabs = (r.nchunks + r.cps - 1) / r.cps;
+    return r;
+}
+
+// Sweeps pipelined behind the host copy (even: the graph's two-sweep body
+// starts at an odd sweep), and the fractions of the slabs after which they
+// advance: every piece of a sweep costs two compaction kernels and five more
+// launches whatever its size, so the early waves are large and the late
+// ones, whose remainder is all that is left once the copy ends, small (a
+// wave per slab piled these fixed costs up behind the copy).
+constexpr int kWaveSweeps = 6;
+constexpr int kWaveEighths[] = {2, 4, 6, 7, 8};
+
+// One-thread bookkeeping between the pieces of the wavefront (kernels rather
+// than small copies or memsets: a device-to-device copy may queue behind the
+// host copies on the copy engine).
+static __global__ void k_wave_mark(LoopState *ls) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) ls->xdone = ls->lc[3];
+}
+static __global__ void k_wave_clear_spills(LoopState *ls) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) ls->lc[2] = 0;
+}
+
+// The host-buffer wavefront.  The copy of slab j + 1 releases the first pass
+// of slab j (sweep 0's detection, complete below plane Z = (j + 1) * slab
+// depth, or nz after the last slab); after the slabs of kWaveEighths follows
+// a wave: on the planes already final, the pieces of sweeps 0 .. K that those
+// planes allow:
+//   sweep k's detection covers planes below D_k, its edits planes below A_k,
+//   with D_0 = Z, A_k = D_k - 1 and D_k = A_{k-1} - 1 (k >= 1),
+// every front reaching nz after the last slab.  Sweep k's detection reads
+// planes up to D_k = A_{k-1} - 1, all edited by sweep k - 1 already; its
+// edits stop one plane below D_k, so no later detection of sweep k reads an
+// edited plane or requests an edit below A_k; the active set of sweep k + 1
+// below D_{k+1} is final once sweep k has edited planes up to D_{k+1} + 1.
+// Each sweep thus sees exactly the field, codes and active set of the
+// snapshot schedule, and sweeps that run while the rest of the field is still
+// crossing the host link leave little to do after it.  Counters go straight
+// to slots[k]; k_wave_gate then sets the loop state as after sweep K.
+template <typename T>
+static int first_pass_waves(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint8_t *cnt, uint32_t *hp,
+                            uint32_t *req, uint32_t *const act[2], SweepSlot *slots, LoopState *ls, const Geom &g,
+                            const FirstMaps &maps, uint32_t *list, uint32_t *xlist, uint32_t *slist, uint32_t *bcnt,
+                            const FastDiv &div_nx, T eps, T delta, int q, int K, cudaStream_t s, int64_t *launches) {
+    if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+    const IngestSlabs sl = ingest_slabs(g, sizeof(T));
+    const int cps = sl.cps, nchunks = sl.nchunks, nslabs = sl.nslabs;
+    const unsigned lb = 152 * 8;
+    struct Res {
+        cudaStream_t cs = nullptr, ds = nullptr;
+        std::vector<cudaEvent_t> ev, evp;
+        ~Res() {  // released once pending work completes
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            for (cudaEvent_t e : evp)
+                if (e) cudaEventDestroy(e);
+            if (cs) cudaStreamDestroy(cs);
+            if (ds) cudaStreamDestroy(ds);
+        }
+    } r;
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.ds, cudaStreamNonBlocking));
+    r.ev.assign(static_cast<size_t>(nslabs) + 1, nullptr);
+    r.evp.assign(static_cast<size_t>(nslabs), nullptr);
+    for (cudaEvent_t &e : r.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaEvent_t &e : r.evp) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
+    PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
+    for (int j = 0; j < nslabs; ++j) {
+        const size_t z0 = static_cast<size_t>(j) * cps * g.zc;
+        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * g.zc);
+        const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
+        PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
+        PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
+        PMSZ_CUDA(cudaEventRecord(r.ev[j], r.cs));
+        if (in.dprev) {  // the pre-correction copy of fhat, before any edit of the slab
+            PMSZ_CUDA(cudaStreamWaitEvent(r.ds, r.ev[j], 0));
+            PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.ds));
+            PMSZ_CUDA(cudaEventRecord(r.evp[j], r.ds));
+        } else {
+            PMSZ_CUDA(cudaEventRecord(r.evp[j], r.cs));
+        }
+    }
+    std::vector<int> Dp(static_cast<size_t>(K) + 1, 0), Ap(static_cast<size_t>(K) + 1, 0);  // fronts so far
+    std::vector<char> wave_after(static_cast<size_t>(nslabs), 0);
+    for (int e : kWaveEighths) wave_after[static_cast<size_t>(std::max(1, (nslabs * e + 7) / 8) - 1)] = 1;
+    for (int j = 0; j < nslabs; ++j) {
+        const bool last = j == nslabs - 1;
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
+        dim3 grid = tiled_grid(g);
+        grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
+        launch_first_pass<T>(maps, grid, s, f, fh, codes, hp, req, act[1], &slots[0], g, j * cps, xlist, &ls->lc[3],
+                             &ls->err);
+        ++*launches;
+        if (!wave_after[static_cast<size_t>(j)]) continue;
+        // the first pass's deferred voxels so far (all below Z), then mark them done
+        k_first_exact<T><<<lb, 256, 0, s>>>(xlist, &ls->lc[3], f, fh, codes, req, act[1], &slots[0], g, div_nx,
+                                            &ls->xdone);
+        k_wave_mark<<<1, 32, 0, s>>>(ls);
+        PMSZ_CUDA(cudaGetLastError());
+        *launches += 2;
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.evp[j], 0));  // fhat's pre-correction copy of slabs 0 .. j
+        const int Z = last ? g.nz : std::min(g.nz, (j + 1) * cps * g.zc);
+        for (int k = 0; k <= K; ++k) {
+            const int D = k == 0 ? Z : (last ? g.nz : std::max(0, Ap[k - 1] - 1));
+            uint32_t *a_next = act[(k + 1) & 1];
+            if (k > 0 && D > Dp[k]) {
+                compact_bitmap_planes(act[k & 1], g, Dp[k], D, bcnt, list, &ls->lc[0], s);
+                k_detect_list<T><<<lb, 256, 0, s>>>(list, &ls->lc[0], fh, hp, codes, req, a_next, slist, &ls->lc[2],
+                                                    &slots[k], g, div_nx, nullptr, &ls->exact_keys, nullptr);
+                k_detect_exact<T><<<lb, 256, 0, s>>>(slist, &ls->lc[2], fh, codes, req, a_next, &slots[k], g, div_nx,
+                                                     nullptr);
+                k_wave_clear_spills<<<1, 32, 0, s>>>(ls);
+                *launches += 5;
+            }
+            Dp[k] = std::max(Dp[k], D);
+            const int A = last ? g.nz : std::max(0, D - 1);
+            if (A > Ap[k]) {
+                compact_bitmap_planes(req, g, Ap[k], A, bcnt, list, &ls->lc[1], s);
+                k_apply_list<T><<<lb, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, a_next, &slots[k], g, div_nx, eps,
+                                                   delta, q, nullptr);
+                *launches += 3;
+                Ap[k] = A;
+            }
+            PMSZ_CUDA(cudaGetLastError());
+        }
+    }
+    return PMSZ_OK;
+}
+
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
                  pmsz_result *res, cudaStream_t s, const HostIngest<T> *ingest) {
@@ -424,6 +565,12 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     const size_t o_xlist = ws.reserve<uint32_t>(use_list ? g.n : 0);
     const size_t o_bcnt = ws.reserve<uint32_t>(use_list ? kCompactBlocks : 0);
     const size_t o_ls = ws.reserve<LoopState>(use_list ? 1 : 0);
+    // host-buffer calls of several slabs run sweeps 1 .. K behind the copy
+    // (first_pass_waves; K even, below max_sweeps); their detection spills go
+    // to a list of their own (xlist still collects the first pass's deferrals)
+    const int wave_k = static_cast<int>(std::min<int64_t>(kWaveSweeps, max_sweeps - 1)) & ~1;
+    const bool waves = ingest && use_list && wave_k >= 2 && ingest_slabs(g, sizeof(T)).nslabs >= 2;
+    const size_t o_slist = ws.reserve<uint32_t>(waves ? g.n : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);
     uint8_t *codes = ws.at<uint8_t>(o_codes);
@@ -435,6 +582,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     uint32_t *xlist = use_list ? ws.at<uint32_t>(o_xlist) : nullptr;
     uint32_t *bcnt = use_list ? ws.at<uint32_t>(o_bcnt) : nullptr;  // per-block counts of a compaction
     LoopState *ls = use_list ? ws.at<LoopState>(o_ls) : nullptr;
+    uint32_t *slist = waves ? ws.at<uint32_t>(o_slist) : nullptr;
     const FastDiv div_nx = make_fastdiv(static_cast<uint32_t>(g.nx));
     const unsigned list_blocks = 152 * 8;
     const FirstMaps maps = use_list ? first_maps<T>(f, fh, g) : FirstMaps{};
@@ -482,27 +630,39 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             if ((rc = lt.init())) return rc;
             PMSZ_CUDA(cudaEventRecord(lt.ev[0], s));
         }
-        if (ingest) {
-            if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches, xlist,
-                                           &ls->lc[3], &maps, &ls->err)))
+        if (waves) {  // sweeps 0 .. wave_k behind the host copy, then the state after them
+            if ((rc = first_pass_waves<T>(*ingest, f, fh, codes, cnt, hp, req, act, slots, ls, g, maps, list, xlist,
+                                          slist, bcnt, div_nx, eps, delta, q, wave_k, s, &launches)))
                 return rc;
-        } else {
-            launch_first_pass<T>(maps, tiled_grid(g), s, f, fh, codes, hp, req, act[1], &ls->cur, g, 0, xlist,
-                                 &ls->lc[3], &ls->err);
+            if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[1], s));
+            k_wave_gate<<<1, 32, 0, s>>>(ls, slots, wave_k, max_sweeps, tail_at, static_cast<unsigned long long>(g.n),
+                                         list_blocks);
             ++launches;
+            PMSZ_CUDA(cudaGetLastError());
+            if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
+        } else {
+            if (ingest) {
+                if ((rc = first_pass_ingest<T>(*ingest, f, fh, codes, hp, req, act[1], &ls->cur, g, s, &launches,
+                                               xlist, &ls->lc[3], &maps, &ls->err)))
+                    return rc;
+            } else {
+                launch_first_pass<T>(maps, tiled_grid(g), s, f, fh, codes, hp, req, act[1], &ls->cur, g, 0, xlist,
+                                     &ls->lc[3], &ls->err);
+                ++launches;
+            }
+            k_first_exact<T><<<list_blocks, 256, 0, s>>>(xlist, &ls->lc[3], f, fh, codes, req, act[1], &ls->cur, g,
+                                                         div_nx);
+            ++launches;
+            if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[1], s));
+            compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, s);
+            k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, act[1], &ls->cur, g, div_nx,
+                                                        eps, delta, q, &ls->go);
+            k_pick_detection<<<1, 32, 0, s>>>(ls, static_cast<unsigned long long>(g.n), list_blocks);
+            k_loop_gate<<<1, 32, 0, s>>>(ls, slots, max_sweeps, tail_at, cudaGraphConditionalHandle{}, 0);
+            launches += 5;
+            PMSZ_CUDA(cudaGetLastError());
+            if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
         }
-        k_first_exact<T><<<list_blocks, 256, 0, s>>>(xlist, &ls->lc[3], f, fh, codes, req, act[1], &ls->cur, g,
-                                                     div_nx);
-        ++launches;
-        if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[1], s));
-        compact_bitmap(req, g, bcnt, list, &ls->lc[1], &ls->go, s);
-        k_apply_list<T><<<list_blocks, 256, 0, s>>>(list, &ls->lc[1], f, fh, cnt, hp, act[1], &ls->cur, g, div_nx, eps,
-                                                    delta, q, &ls->go);
-        k_pick_detection<<<1, 32, 0, s>>>(ls, static_cast<unsigned long long>(g.n), list_blocks);
-        k_loop_gate<<<1, 32, 0, s>>>(ls, slots, max_sweeps, tail_at, cudaGraphConditionalHandle{}, 0);
-        launches += 5;
-        PMSZ_CUDA(cudaGetLastError());
-        if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[2], s));
 
         // One body: two list sweeps (odd: act[1] -> act[0], even: act[0] ->
         // act[1]), each ending with k_loop_gate; with set_cond the second gate
@@ -576,7 +736,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         if (hls->err)
             return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
         const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
-        const int64_t nloop = std::max<int64_t>(done - 1, 0);
+        const int64_t nloop = std::max<int64_t>(done - (waves ? wave_k + 1 : 1), 0);  // sweeps of the loop
         launches += 16 * ((flags & PMSZ_FLAG_HOST_LOOP) ? bodies : std::max<int64_t>(1, (nloop + 1) / 2));
         if (timing) {  // the list sweeps' edits run inside the graph and count as detection time
             float a = 0, b = 0, c = 0;

@@ -33,8 +33,9 @@ constexpr int kCompactWords = kCompactBlock * 4;  // one uint4 of words per thre
 // writes the flat indices of its range in order and clears the words.  Block b
 // of both kernels covers words [b * per, (b + 1) * per), per a multiple of 4.
 
-__host__ __device__ __forceinline__ size_t compact_per(const Geom &g) {
-    return ((g.nwords + kCompactBlocks - 1) / kCompactBlocks + 3) & ~static_cast<size_t>(3);
+// Words per block of a compaction launched with `blocks` blocks.
+__host__ __device__ __forceinline__ size_t compact_per(const Geom &g, size_t blocks) {
+    return ((g.nwords + blocks - 1) / blocks + 3) & ~static_cast<size_t>(3);
 }
 
 __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t *s_warp) {
@@ -48,19 +49,27 @@ __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t *s_warp) 
     return tot;
 }
 
+// Both compaction kernels read g.nwords words from bm; a z-range of a bitmap
+// is passed as bm + wbase (wbase a multiple of 4, for the 16-byte loads) with
+// g.nwords the range's length from there, and `skip` (< 4) words at its start
+// that belong to the plane before the range: they are neither listed nor
+// cleared.  List entries are absolute voxel indices.  The block count is the
+// launch's (compact_per).
 static __global__ void __launch_bounds__(kCompactBlock) k_count_words(const uint32_t *__restrict__ bm, Geom g,
-                                                               uint32_t *__restrict__ counts, const int *run) {
+                                                               uint32_t *__restrict__ counts, const int *run,
+                                                               uint32_t skip = 0) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
     if (run && *run == 0) return;
-    const size_t per = compact_per(g);
+    const size_t per = compact_per(g, gridDim.x);
     const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(g.nwords, lo + per);
     uint32_t c = 0;
     for (size_t w0 = lo + static_cast<size_t>(threadIdx.x) * 4; w0 < hi; w0 += kCompactWords) {
-        if (w0 + 4 <= hi) {
+        if (w0 + 4 <= hi && w0 >= skip) {
             const uint4 v = *reinterpret_cast<const uint4 *>(bm + w0);
             c += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         } else {
-            for (size_t w = w0; w < hi; ++w) c += __popc(bm[w]);
+            for (size_t w = w0; w < hi && w < w0 + 4; ++w)
+                if (w >= skip) c += __popc(bm[w]);
         }
     }
     c = block_sum_u32(c, s_warp);
@@ -130,7 +139,8 @@ __device__ __forceinline__ void write_step_entries(const uint32_t (&w)[4], uint3
 static __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *__restrict__ bm, Geom g,
                                                               const uint32_t *__restrict__ counts,
                                                               uint32_t *__restrict__ list, uint32_t *total,
-                                                              const int *run) {
+                                                              const int *run, uint32_t wbase = 0,
+                                                              uint32_t skip = 0) {
     __shared__ uint32_t s_warp[kCompactBlock / 32];
     __shared__ __align__(16) unsigned char s_raw[kStageBytes];
     if (run && *run == 0) return;
@@ -144,19 +154,19 @@ static __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *_
     uint32_t pos = block_sum_u32(before, s_warp);
     all = block_sum_u32(all, s_warp);
     if (blockIdx.x == 0 && t == 0) *total = all;
-    const size_t per = compact_per(g);
+    const size_t per = compact_per(g, gridDim.x);
     const size_t lo = static_cast<size_t>(blockIdx.x) * per, hi = min(g.nwords, lo + per);
     for (size_t base = lo; base < hi; base += kCompactWords) {
         const size_t w0 = base + static_cast<size_t>(t) * 4;
         uint32_t w[4] = {0u, 0u, 0u, 0u};
-        if (w0 + 4 <= hi) {
+        if (w0 + 4 <= hi && w0 >= skip) {
             const uint4 v = *reinterpret_cast<const uint4 *>(bm + w0);
             w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
             if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4 *>(bm + w0) = make_uint4(0, 0, 0, 0);
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                if (w0 + j < hi) {
+                if (w0 + j < hi && w0 + j >= skip) {
                     w[j] = bm[w0 + j];
                     if (w[j]) bm[w0 + j] = 0;
                 }
@@ -171,14 +181,14 @@ static __global__ void __launch_bounds__(kCompactBlock) k_write_list(uint32_t *_
         }
         if (lane == 31) s_warp[warp] = inc;
         __syncthreads();
-        uint32_t wbase = 0, step = 0;
+        uint32_t wbase_warp = 0, step = 0;
         for (int k = 0; k < kCompactBlock / 32; ++k) {
             const uint32_t u = s_warp[k];
-            if (k < warp) wbase += u;
+            if (k < warp) wbase_warp += u;
             step += u;
         }
-        const uint32_t mine = static_cast<uint32_t>(w0);  // nwords < 2^27 in the list form
-        write_step_entries(w, inc - c, wbase, step, s_raw, list + pos, [&](int j) {
+        const uint32_t mine = wbase + static_cast<uint32_t>(w0);  // nwords < 2^27 in the list form
+        write_step_entries(w, inc - c, wbase_warp, step, s_raw, list + pos, [&](int j) {
             const uint32_t wj = mine + static_cast<uint32_t>(j);
             const uint32_t row = fdiv(wj, g.div_wpr);
             const uint32_t wx = wj - row * static_cast<uint32_t>(g.wpr);
@@ -358,12 +368,12 @@ __global__ void __launch_bounds__(256) k_first_exact(const uint32_t *__restrict_
                                                      const T *__restrict__ f, const T *__restrict__ fh,
                                                      uint8_t *__restrict__ codes, uint32_t *__restrict__ req,
                                                      uint32_t *__restrict__ act_next, SweepSlot *slot, Geom g,
-                                                     FastDiv div_nx) {
-    const uint32_t m = *count;
+                                                     FastDiv div_nx, const uint32_t *start = nullptr) {
+    const uint32_t m = *count, m0 = start ? *start : 0u;  // entries m0 .. m-1
     uint32_t cmax = 0, cmin = 0, cdir = 0;
     const ptrdiff_t sy = g.nx, sz = static_cast<ptrdiff_t>(g.nx) * g.ny;
     using K = typename KeyOf<T>::type;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    for (uint32_t k = m0 + blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
         const uint32_t i = __ldg(xlist + k);
         int x, y, z;
         voxel_coords(g, div_nx, i, x, y, z);
@@ -453,6 +463,22 @@ inline void compact_bitmap(uint32_t *bm, const Geom &g, uint32_t *counts, uint32
     k_write_list<<<kCompactBlocks, kCompactBlock, 0, s>>>(bm, g, counts, list, total, run);
 }
 
+// The same over the planes [z0, z1) of the bitmap (z0 < z1), with at most a
+// block per step of words (a z-range is often a small part of the bitmap).
+inline void compact_bitmap_planes(uint32_t *bm, const Geom &g, int z0, int z1, uint32_t *counts, uint32_t *list,
+                                  uint32_t *total, cudaStream_t s) {
+    const size_t wpp = static_cast<size_t>(g.wpr) * g.ny;  // words per plane
+    const size_t first = static_cast<size_t>(z0) * wpp, base = first & ~static_cast<size_t>(3);
+    Geom r = g;
+    r.nwords = static_cast<size_t>(z1) * wpp - base;
+    const uint32_t skip = static_cast<uint32_t>(first - base);
+    const unsigned blocks = static_cast<unsigned>(
+        std::min<size_t>(kCompactBlocks, (r.nwords + kCompactWords - 1) / kCompactWords));
+    k_count_words<<<blocks, kCompactBlock, 0, s>>>(bm + base, r, counts, nullptr, skip);
+    k_write_list<<<blocks, kCompactBlock, 0, s>>>(bm + base, r, counts, list, total, nullptr,
+                                                   static_cast<uint32_t>(base), skip);
+}
+
 // State of the device-side sweep loop: the index of the sweep that runs
 // next, its gate, its list lengths and its counters (copied to the sweep's
 // slot by k_loop_gate).
@@ -463,6 +489,7 @@ struct LoopState {
     uint32_t lc[4];  // active list, request list, exact list (spills), first-pass deferrals
     uint32_t deferred;  // voxels of the current list sweep decided on exact keys
     uint32_t err;    // set by the first pass when a tensor copy did not arrive
+    uint32_t xdone;  // first-pass deferrals already decided (the host-buffer wavefront)
     SweepSlot cur;
 };
 
@@ -507,6 +534,40 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
         ls->deferred = 0;
     }
     if (set_cond) cudaGraphSetConditional(cond, ls->go ? 1u : 0u);
+}
+
+// After the host-buffer wavefront has run sweeps 0 .. K to the end: the loop
+// state that k_loop_gate would have left after sweep K, or after the first of
+// those sweeps that stops the loop (the sweeps after a stopping one changed
+// nothing: they found an empty active set, or repeated a sweep whose edits
+// changed no value and no counter, or follow a NaN input whose call fails),
+// and k_pick_detection's choice from sweep 0.
+static __global__ void k_wave_gate(LoopState *ls, const SweepSlot *slots, long long K, long long max_sweeps,
+                                   unsigned long long tail_at, unsigned long long n, unsigned long long blocks) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long k = 0;
+    bool stop = false;
+    for (; k <= K; ++k) {
+        const SweepSlot c = slots[k];
+        stop = (k == 0 && c.bad) || (c.fmax == 0 && c.fmin == 0 && c.fdir == 0) || c.progressed == 0 ||
+               k + 1 >= max_sweeps;
+        if (stop) break;
+    }
+    if (stop) {
+        ls->k = k + 1;
+        ls->go = 0;
+    } else {
+        const SweepSlot c = slots[K];
+        ls->k = K + 1;
+        ls->go = 15ull * c.changed + c.fdir <= tail_at ? 0 : 1;
+    }
+    const unsigned long long deferred = ls->lc[3];
+    const unsigned long long est = 15ull * slots[0].changed + slots[0].fdir;
+    const double spill = static_cast<double>(deferred) * static_cast<double>(est) / static_cast<double>(n);
+    if (10ull * deferred > n || spill > 0.5 * kExactCap * static_cast<double>(blocks)) ls->exact_keys = 1;
+    ls->cur = SweepSlot{};
+    ls->lc[0] = ls->lc[1] = ls->lc[2] = ls->lc[3] = 0;
+    ls->deferred = 0;
 }
 
 }  // namespace pmsz

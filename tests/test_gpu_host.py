@@ -193,3 +193,51 @@ def test_cli_edit_files_match_the_reference_encoder(cuda, tmp_path, name):
                                   A.decode_clamps(ref_e, np.float64).view(np.uint8))
     if A.zstd_version() == int(cases["zstd_version"]):
         assert blob_d == ref_d and blob_e == ref_e
+
+
+# Fields of several 64 MiB copy slabs run sweeps 1..6 behind the host copy
+# (each sweep two planes behind the one before); max_sweeps 2, 3 and 5 cut the
+# pipelined sweeps short (K = 0 / 2 / 4), sz3 plateaus defer many voxels.
+WAVE_CASES = [
+    ((384, 256, 256), torch.float64, "zfp", 1e-4, 10000, 61),   # 6 slabs of 64 planes
+    ((384, 256, 256), torch.float32, "sz3", 1e-3, 10000, 62),   # 3 slabs of 128 planes
+    ((400, 256, 256), torch.float32, "zfp", 1e-2, 10000, 63),   # a short last slab, many clamps
+    ((96, 256, 256), torch.float64, "zfp", 1e-4, 10000, 68),    # two slabs: waves after both
+    ((384, 256, 256), torch.float64, "zfp", 1e-4, 2, 64),
+    ((384, 256, 256), torch.float64, "zfp", 1e-4, 3, 65),
+    ((384, 256, 256), torch.float64, "sz3", 1e-3, 5, 66),
+]
+
+
+@pytest.mark.parametrize("case", WAVE_CASES, ids=lambda c: f"{c[0][0]}-{str(c[1])[6:]}-{c[2]}-max{c[4]}")
+def test_host_wavefront_matches_device_call(cuda, case):
+    shape, dt, comp, eb, max_sweeps, seed = case
+    A = api()
+    f = A.gen_perlin(shape, seed, 5, 1 / 32, dtype=dt, device=cuda)
+    fh = A.standin(f, eb, comp, seed)
+    ref = fh.clone()
+    r = A.correct(f, ref, eb, max_sweeps=max_sweeps)
+    hf, hfh = f.cpu().pin_memory(), fh.cpu().pin_memory()
+    work = hfh.clone().pin_memory()
+    rh, _ = A.correct_host(hf, work, eb, max_sweeps=max_sweeps)
+    assert (rh.status, rh.sweeps, rh.iteration, rh.edits) == (r.status, r.sweeps, r.iteration, r.edits)
+    np.testing.assert_array_equal(rh.log, r.log)
+    assert torch.equal(work.view(torch.uint8), ref.cpu().view(torch.uint8))
+    if max_sweeps == 10000:
+        assert r.status == capi.PMSZ_OK and r.sweeps > 7  # the pipeline ran to its depth and beyond
+
+
+def test_host_wavefront_nan_input_fails_like_the_device_call(cuda):
+    A = api()
+    shape, eb = (384, 256, 256), 1e-3
+    f = A.gen_perlin(shape, 67, 4, 1 / 32, dtype=torch.float32, device=cuda)
+    fh = A.standin(f, eb, "zfp", 67)
+    fh[300, 7, 9] = float("nan")  # in the third slab: the first ones ran their sweeps already
+    with pytest.raises(capi.PmszError) as dev:
+        A.correct(f, fh.clone(), eb)
+    hfh = fh.cpu().pin_memory()
+    work = hfh.clone().pin_memory()
+    with pytest.raises(capi.PmszError) as host:
+        A.correct_host(f.cpu().pin_memory(), work, eb)
+    assert host.value.status == dev.value.status == capi.PMSZ_ERR_ARG
+    assert torch.equal(work.view(torch.uint8), hfh.view(torch.uint8))  # the caller's buffer is left as it was
