@@ -410,7 +410,10 @@ static IngestSlabs ingest_slabs(const Geom &g, size_t elem) {
 // ones, whose remainder is all that is left once the copy ends, small (a
 // wave per slab piled these fixed costs up behind the copy).
 constexpr int kWaveSweeps = 6;
-constexpr int kWaveEighths[] = {2, 4, 6, 7, 8};
+// in sixteenths of the slabs; fp32 slabs cross the link in half the time of
+// fp64 slabs of as many voxels, while the sweeps cost about the same
+constexpr int kWaveAt8[] = {4, 8, 12, 14, 16};
+constexpr int kWaveAt4[] = {4, 8, 12, 16};
 
 // One-thread bookkeeping between the pieces of the wavefront (kernels rather
 // than small copies or memsets: a device-to-device copy may queue behind the
@@ -424,8 +427,8 @@ static __global__ void k_wave_clear_spills(LoopState *ls) {
 
 // The host-buffer wavefront.  The copy of slab j + 1 releases the first pass
 // of slab j (sweep 0's detection, complete below plane Z = (j + 1) * slab
-// depth, or nz after the last slab); after the slabs of kWaveEighths follows
-// a wave: on the planes already final, the pieces of sweeps 0 .. K that those
+// depth, or nz after the last slab); after the slabs of kWaveAt8 / kWaveAt4
+// follows a wave: on the planes already final, the pieces of sweeps 0 .. K that those
 // planes allow:
 //   sweep k's detection covers planes below D_k, its edits planes below A_k,
 //   with D_0 = Z, A_k = D_k - 1 and D_k = A_{k-1} - 1 (k >= 1),
@@ -485,7 +488,11 @@ static int first_pass_waves(const HostIngest<T> &in, const T *f, T *fh, uint8_t 
     }
     std::vector<int> Dp(static_cast<size_t>(K) + 1, 0), Ap(static_cast<size_t>(K) + 1, 0);  // fronts so far
     std::vector<char> wave_after(static_cast<size_t>(nslabs), 0);
-    for (int e : kWaveEighths) wave_after[static_cast<size_t>(std::max(1, (nslabs * e + 7) / 8) - 1)] = 1;
+    auto mark = [&](int e) { wave_after[static_cast<size_t>(std::max(1, (nslabs * e + 15) / 16) - 1)] = 1; };
+    if (sizeof(T) == 8)
+        for (int e : kWaveAt8) mark(e);
+    else
+        for (int e : kWaveAt4) mark(e);
     for (int j = 0; j < nslabs; ++j) {
         const bool last = j == nslabs - 1;
         PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
