@@ -75,15 +75,20 @@ __device__ __forceinline__ bool fp_lt(T a, T b) {
 // tile: the clamp flags (one word per 32 voxels, set in shared memory), the
 // clamp count and the edit count, combined in shared memory (no global
 // atomics: one counter shared by every warp serialises at L2).
-template <typename T>
+// PACK: the symbols are not stored one byte per voxel but staged in shared
+// memory and written packed at nbits bits each (thread t of the grid: symbols
+// 8t .. 8t+7 in bytes nbits*t .. nbits*t + nbits - 1, pack_nbits' layout, as
+// k_pack_deltas writes it from the unpacked array).
+template <typename T, bool PACK>
 __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, const T *__restrict__ cur,
                                                  const T *__restrict__ f, const uint8_t *__restrict__ cnt, size_t n,
                                                  T eps, T delta, T inv, T quarter, int q, uint8_t *__restrict__ deltas,
                                                  uint32_t *__restrict__ flags, uint32_t *__restrict__ tile_count,
-                                                 uint32_t *__restrict__ tile_edits) {
+                                                 uint32_t *__restrict__ tile_edits, int nbits, size_t packed_len) {
     __shared__ uint32_t s_cnt, s_edits;
     __shared__ uint32_t s_fl[kTile / 32];
     __shared__ uint16_t s_list[8][kTile / 8];  // per warp: changed voxels, offsets within the tile
+    __shared__ __align__(8) uint8_t s_sym[PACK ? kTile : 8];  // PACK: the tile's symbols
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_cnt = s_edits = 0;
     if (threadIdx.x < kTile / 32) s_fl[threadIdx.x] = 0;
@@ -93,7 +98,7 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
     // delta store); the values of the touched ones are loaded together
     const uint32_t off0 = static_cast<uint32_t>(threadIdx.x) * 8;
     const size_t i0 = base + off0;
-    const bool full = i0 + 8 <= n && (reinterpret_cast<uintptr_t>(deltas + i0) & 7) == 0 &&
+    const bool full = i0 + 8 <= n && (PACK || (reinterpret_cast<uintptr_t>(deltas + i0) & 7) == 0) &&
                       (!cnt || (reinterpret_cast<uintptr_t>(cnt + i0) & 7) == 0);
     uint8_t cv[8];
     if (full && cnt) {
@@ -114,7 +119,9 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
 #pragma unroll
     for (int j = 0; j < 8; ++j)
         if (cv[j] && !fp_eq(c8[j], p8[j])) needm |= 1u << j;
-    if (full) {  // unchanged voxels: delta 0; changed ones are written below
+    if (PACK) {  // unchanged voxels: symbol 0 (the warp's changed ones are written below)
+        *reinterpret_cast<uint2 *>(s_sym + off0) = make_uint2(0u, 0u);
+    } else if (full) {  // unchanged voxels: delta 0; changed ones are written below
         if (needm != 0xFFu) *reinterpret_cast<uint2 *>(deltas + i0) = make_uint2(0u, 0u);
     } else {
 #pragma unroll
@@ -151,7 +158,23 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
                     ++clamps;
                 }
             }
-            deltas[i] = d;
+            if (PACK) s_sym[off] = d;
+            else deltas[i] = d;
+        }
+    }
+    if (PACK) {  // this thread's 8 symbols (all written by its own warp) -> nbits bytes
+        __syncwarp();
+        if (i0 < n) {
+            const uint2 u = *reinterpret_cast<const uint2 *>(s_sym + off0);
+            const uint64_t mask = (1ull << nbits) - 1ull;
+            uint64_t v = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const uint64_t sym = ((j < 4 ? u.x : u.y) >> ((j & 3) * 8)) & 0xFFu;
+                if (i0 + j < n) v |= (sym & mask) << (j * nbits);
+            }
+            const size_t b0 = (i0 >> 3) * static_cast<size_t>(nbits);
+            for (int b = 0; b < nbits && b0 + b < packed_len; ++b) deltas[b0 + b] = static_cast<uint8_t>(v >> (8 * b));
         }
     }
     clamps = warp_sum_u32(clamps);
@@ -169,29 +192,72 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
     }
 }
 
-// Exclusive scan of `m` tile clamp counts in one block of 1024 threads (total
-// in total[0]) and the sum of the tile edit counts (total[1]).
-__global__ void __launch_bounds__(1024) k_scan_tiles(uint32_t *__restrict__ counts,
-                                                     const uint32_t *__restrict__ edits, size_t m,
-                                                     unsigned long long *total) {
-    // chunks of 1024 entries, one per thread (coalesced): warp scans, then the
-    // warps' totals, then the running offset of the chunks before
+// Exclusive scan of the `m` tile clamp counts in two levels: k_scan_part
+// scans chunks of 1024 tiles in place (one block each) and stores each
+// chunk's clamp and edit sums; k_scan_chunks scans the chunk sums in one
+// block (offsets in part[0 .. nc), the clamp total in total[0], the edit total
+// in total[1]); a tile's offset is then counts[t] + part[t >> 10].
+constexpr int kScanChunk = 1024;
+__global__ void __launch_bounds__(kScanChunk) k_scan_part(uint32_t *__restrict__ counts,
+                                                          const uint32_t *__restrict__ edits, size_t m,
+                                                          uint32_t *__restrict__ part, unsigned long long *epart) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ unsigned long long s_e[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t i = static_cast<size_t>(blockIdx.x) * kScanChunk + threadIdx.x;
+    const uint32_t v = i < m ? counts[i] : 0u;
+    unsigned long long e = i < m ? edits[i] : 0ull;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+    if (lane == 31) s_warp[warp] = inc;
+    if (lane == 0) s_e[warp] = e;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t wv = s_warp[lane];
+        uint32_t winc = wv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, winc, o);
+            if (lane >= o) winc += t;
+        }
+        s_warp[lane] = winc - wv;  // exclusive offsets of the warps
+        unsigned long long es = s_e[lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) es += __shfl_xor_sync(0xFFFFFFFFu, es, o);
+        if (lane == 31) {
+            part[blockIdx.x] = winc;  // the chunk's clamp sum
+            epart[blockIdx.x] = es;
+        }
+    }
+    __syncthreads();
+    if (i < m) counts[i] = s_warp[warp] + inc - v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_chunks(uint32_t *__restrict__ part,
+                                                      const unsigned long long *__restrict__ epart, size_t nc,
+                                                      unsigned long long *total) {
     __shared__ unsigned long long s_warp[32];
     __shared__ unsigned long long s_run;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_run = 0;
     unsigned long long esum = 0;
-    for (size_t c0 = 0; c0 < m; c0 += 1024) {
+    for (size_t c0 = 0; c0 < nc; c0 += 1024) {  // at most 2^32 / 2^21 = 2048 chunks: two rounds
         const size_t i = c0 + threadIdx.x;
-        const unsigned long long v = i < m ? counts[i] : 0ull;
-        if (i < m) esum += edits[i];
+        const unsigned long long v = i < nc ? part[i] : 0ull;
+        if (i < nc) esum += epart[i];
         unsigned long long inc = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
             if (lane >= o) inc += t;
         }
-        __syncthreads();  // s_warp / s_run of the previous chunk are consumed
+        __syncthreads();  // s_warp / s_run of the previous round are consumed
         if (lane == 31) s_warp[warp] = inc;
         __syncthreads();
         if (warp == 0) {
@@ -202,11 +268,11 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(uint32_t *__restrict__ coun
                 const unsigned long long t = __shfl_up_sync(0xFFFFFFFFu, winc, o);
                 if (lane >= o) winc += t;
             }
-            s_warp[lane] = winc - wv;  // exclusive offsets of the warps
+            s_warp[lane] = winc - wv;
         }
         __syncthreads();
         const unsigned long long run = s_run;
-        if (i < m) counts[i] = static_cast<uint32_t>(run + s_warp[warp] + inc - v);  // at most n < 2^32 clamp values
+        if (i < nc) part[i] = static_cast<uint32_t>(run + s_warp[warp] + inc - v);  // at most n < 2^32 clamps
         __syncthreads();
         if (threadIdx.x == 1023) s_run = run + s_warp[31] + inc;
     }
@@ -227,7 +293,8 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(uint32_t *__restrict__ coun
 // tile's offset plus its rank: clamp values in voxel order.
 template <typename T>
 __global__ void __launch_bounds__(256) k_scatter_clamps(const T *__restrict__ cur, const uint32_t *__restrict__ flags,
-                                                        const uint32_t *__restrict__ tile_off, size_t n, size_t tiles,
+                                                        const uint32_t *__restrict__ tile_off,
+                                                        const uint32_t *__restrict__ part, size_t n, size_t tiles,
                                                         T *__restrict__ clamp) {
     const size_t tile = static_cast<size_t>(blockIdx.x) * 8 + (threadIdx.x >> 5);
     if (tile >= tiles) return;
@@ -244,24 +311,49 @@ __global__ void __launch_bounds__(256) k_scatter_clamps(const T *__restrict__ cu
         const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
         if (lane >= o) inc += t;
     }
-    uint32_t pos = tile_off[tile] + inc - c;
+    uint32_t pos = tile_off[tile] + part[tile / kScanChunk] + inc - c;
     for (uint32_t bits = a; bits; bits &= bits - 1) clamp[pos++] = cur[base + w0 * 32 + (__ffs(bits) - 1)];
     for (uint32_t bits = b; bits; bits &= bits - 1) clamp[pos++] = cur[base + (w0 + 1) * 32 + (__ffs(bits) - 1)];
 }
 
+// Scratch of the two-level tile scan.
+struct TileScan {
+    size_t chunks;
+    size_t o_part, o_epart;
+};
+static TileScan reserve_tile_scan(Workspace &ws, size_t tiles) {
+    TileScan t;
+    t.chunks = (tiles + kScanChunk - 1) / kScanChunk;
+    t.o_part = ws.reserve<uint32_t>(t.chunks);
+    t.o_epart = ws.reserve<unsigned long long>(t.chunks);
+    return t;
+}
+static void launch_tile_scan(Workspace &ws, const TileScan &t, uint32_t *counts, const uint32_t *second, size_t tiles,
+                             unsigned long long *tot, cudaStream_t s) {
+    k_scan_part<<<static_cast<unsigned>(t.chunks), kScanChunk, 0, s>>>(counts, second, tiles, ws.at<uint32_t>(t.o_part),
+                                                                        ws.at<unsigned long long>(t.o_epart));
+    k_scan_chunks<<<1, 1024, 0, s>>>(ws.at<uint32_t>(t.o_part), ws.at<unsigned long long>(t.o_epart), t.chunks, tot);
+}
+
+// Enqueues the extraction on s; the clamp and edit totals land in host[0]
+// and host[1] (pinned) once the stream reaches that point.  packed (or
+// null): the symbols packed at nbits bits each instead of one byte per voxel
+// in deltas.  The scratch is released stream-ordered before return.
 template <typename T>
-int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas, T *clamp,
-                 uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s, const uint8_t *cnt) {
-    if (!prev || !cur || !f || !deltas || !clamp || !n_clamp || !edit_count)
-        return set_error(PMSZ_ERR_ARG, "null pointer");
+int extract_enqueue(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas,
+                    uint8_t *packed, int nbits, T *clamp, unsigned long long *host, cudaStream_t s,
+                    const uint8_t *cnt) {
+    if (!prev || !cur || !f || !(deltas || packed) || !clamp || !host) return set_error(PMSZ_ERR_ARG, "null pointer");
     if (n == 0 || n >= (static_cast<size_t>(1) << 32)) return set_error(PMSZ_ERR_ARG, "n must be in 1..2^32-1");
     if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
     if (!(eb > 0.0)) return set_error(PMSZ_ERR_ARG, "error bound must be positive");
+    if (packed && (nbits < 1 || nbits > 8)) return set_error(PMSZ_ERR_ARG, "symbol width must be 1..8 bits");
     const size_t tiles = (n + kTile - 1) / kTile;
     Workspace ws(s);
     const size_t o_flags = ws.reserve<uint32_t>(tiles * (kTile / 32));
     const size_t o_tiles = ws.reserve<uint32_t>(tiles), o_tedits = ws.reserve<uint32_t>(tiles);
     const size_t o_tot = ws.reserve<unsigned long long>(2);
+    const TileScan ts = reserve_tile_scan(ws, tiles);
     int rc = ws.commit();
     if (rc) return rc;
     uint32_t *flags = ws.at<uint32_t>(o_flags), *tc = ws.at<uint32_t>(o_tiles), *te = ws.at<uint32_t>(o_tedits);
@@ -269,18 +361,33 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
     const T eps = static_cast<T>(eb);
     const T delta = static_cast<T>(eb / static_cast<double>(q));
     const T inv = static_cast<T>(1.0 / static_cast<double>(delta)), quarter = static_cast<T>(0.25 * static_cast<double>(delta));
-    k_extract<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, cur, f, cnt, n, eps, delta, inv, quarter, q, deltas,
-                                                              flags, tc, te);
-    k_scan_tiles<<<1, 1024, 0, s>>>(tc, te, tiles, tot);
-    k_scatter_clamps<T><<<static_cast<unsigned>((tiles + 7) / 8), 256, 0, s>>>(cur, flags, tc, n, tiles, clamp);
+    if (packed)
+        k_extract<T, true><<<static_cast<unsigned>(tiles), 256, 0, s>>>(
+            prev, cur, f, cnt, n, eps, delta, inv, quarter, q, packed, flags, tc, te, nbits,
+            (n * static_cast<size_t>(nbits) + 7) / 8);
+    else
+        k_extract<T, false><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, cur, f, cnt, n, eps, delta, inv,
+                                                                         quarter, q, deltas, flags, tc, te, 8, 0);
+    launch_tile_scan(ws, ts, tc, te, tiles, tot, s);
+    k_scatter_clamps<T><<<static_cast<unsigned>((tiles + 7) / 8), 256, 0, s>>>(cur, flags, tc, ws.at<uint32_t>(ts.o_part),
+                                                                              n, tiles, clamp);
     PMSZ_CUDA(cudaGetLastError());
+    PMSZ_CUDA(cudaMemcpyAsync(host, tot, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    return ws.release();
+}
+
+template <typename T>
+int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas, T *clamp,
+                 uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s, const uint8_t *cnt) {
+    if (!deltas || !n_clamp || !edit_count) return set_error(PMSZ_ERR_ARG, "null pointer");
     unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
     if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
-    PMSZ_CUDA(cudaMemcpyAsync(h, tot, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    int rc = extract_enqueue<T>(prev, cur, f, n, eb, q, deltas, nullptr, 8, clamp, h, s, cnt);
+    if (rc) return rc;
     PMSZ_CUDA(cudaStreamSynchronize(s));
     *n_clamp = h[0];
     *edit_count = h[1];
-    return ws.release();
+    return PMSZ_OK;
 }
 
 // Thread t packs symbols 8t .. 8t+7 (8 * nbits bits = nbits whole bytes).
@@ -376,7 +483,8 @@ __global__ void __launch_bounds__(256) k_recon_flags(const uint8_t *__restrict__
 template <typename T>
 __global__ void __launch_bounds__(256) k_recon_apply(const T *prev, const uint8_t *__restrict__ deltas,
                                                      const T *__restrict__ clamp, const uint32_t *__restrict__ flags,
-                                                     const uint32_t *__restrict__ tile_off, size_t n, T delta, int q,
+                                                     const uint32_t *__restrict__ tile_off,
+                                                     const uint32_t *__restrict__ part, size_t n, T delta, int q,
                                                      T *out) {
     __shared__ uint32_t s_fl[kTile / 32], s_pre[kTile / 32];
     const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
@@ -396,7 +504,7 @@ __global__ void __launch_bounds__(256) k_recon_apply(const T *prev, const uint8_
         s_pre[2 * lane + 1] = inc - b;
     }
     __syncthreads();
-    const uint32_t t0 = tile_off[blockIdx.x];
+    const uint32_t t0 = tile_off[blockIdx.x] + part[blockIdx.x / kScanChunk];
     // consecutive threads, consecutive voxels; all eight symbols and values
     // are loaded before any is used, so their loads are in flight together
     int d8[8];
@@ -439,12 +547,13 @@ int reconstruct_impl(const T *prev, const uint8_t *deltas, const T *clamp, uint6
     const size_t o_flags = ws.reserve<uint32_t>(tiles * (kTile / 32));
     const size_t o_tiles = ws.reserve<uint32_t>(tiles), o_bad = ws.reserve<uint32_t>(tiles);
     const size_t o_tot = ws.reserve<unsigned long long>(2);
+    const TileScan ts = reserve_tile_scan(ws, tiles);
     int rc = ws.commit();
     if (rc) return rc;
     uint32_t *flags = ws.at<uint32_t>(o_flags), *tc = ws.at<uint32_t>(o_tiles), *tb = ws.at<uint32_t>(o_bad);
     unsigned long long *tot = ws.at<unsigned long long>(o_tot);
     k_recon_flags<<<static_cast<unsigned>(tiles), 256, 0, s>>>(deltas, n, q, flags, tc, tb);
-    k_scan_tiles<<<1, 1024, 0, s>>>(tc, tb, tiles, tot);
+    launch_tile_scan(ws, ts, tc, tb, tiles, tot, s);
     PMSZ_CUDA(cudaGetLastError());
     unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
     if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
@@ -460,11 +569,16 @@ int reconstruct_impl(const T *prev, const uint8_t *deltas, const T *clamp, uint6
                                            std::to_string(n_clamp) + " values");
     }
     const T delta = static_cast<T>(eb / static_cast<double>(q));
-    k_recon_apply<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, deltas, clamp, flags, tc, n, delta, q, out);
+    k_recon_apply<T><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, deltas, clamp, flags, tc,
+                                                                  ws.at<uint32_t>(ts.o_part), n, delta, q, out);
     PMSZ_CUDA(cudaGetLastError());
     return ws.release();
 }
 
+template int extract_enqueue<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *,
+                                    uint8_t *, int, float *, unsigned long long *, cudaStream_t, const uint8_t *);
+template int extract_enqueue<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,
+                                     uint8_t *, int, double *, unsigned long long *, cudaStream_t, const uint8_t *);
 template int extract_impl<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *, float *,
                                  uint64_t *, uint64_t *, cudaStream_t, const uint8_t *);
 template int extract_impl<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,

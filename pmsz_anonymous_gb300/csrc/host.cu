@@ -22,12 +22,12 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     const bool want_verify = outs && outs->verify;
     const int q = opts ? opts->q : 5;
     Workspace ws(s);
+    const bool packed = opts && (opts->flags & PMSZ_FLAG_PACKED_DELTAS) && outs && outs->deltas;
     const size_t o_f = ws.reserve<T>(n), o_fh = ws.reserve<T>(n);
     const size_t o_prev = ws.reserve<T>(want_edits ? n : 0);
-    const size_t o_d = ws.reserve<uint8_t>(want_edits ? n : 0);
+    const size_t o_d = ws.reserve<uint8_t>(want_edits && !packed ? n : 0);
     const size_t o_c = ws.reserve<T>(want_edits ? n : 0);
     const size_t o_cnt = ws.reserve<uint8_t>(want_edits ? n : 0);
-    const bool packed = opts && (opts->flags & PMSZ_FLAG_PACKED_DELTAS) && outs && outs->deltas;
     const int nbits = q >= 1 && q <= 255 ? bits_for_symbols(q) : 8;  // q is checked by the correction
     const size_t plen = packed ? (n * static_cast<size_t>(nbits) + 7) / 8 : 0;
     const size_t o_pack = ws.reserve<uint8_t>(plen);
@@ -50,19 +50,21 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
     std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
     if (want_edits) {
-        uint64_t nc = 0, ec = 0;
+        // the symbols (packed on the GPU at nbits bits, the reference's
+        // pack_nbits, when asked: n * nbits / 8 bytes cross the host link) go
+        // back while the host waits for the clamp count
         const bool counted = !(opts && (opts->flags & PMSZ_FLAG_NAIVE));  // the pMSz loop left its counters in dcnt
-        if ((rc = extract_impl<T>(dprev, dfh, df, n, eb, q, dd, dclamp, &nc, &ec, s, counted ? dcnt : nullptr)))
+        unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
+        if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+        uint8_t *dp = packed ? ws.at<uint8_t>(o_pack) : nullptr;
+        if ((rc = extract_enqueue<T>(dprev, dfh, df, n, eb, q, dd, dp, nbits, dclamp, h, s, counted ? dcnt : nullptr)))
             return rc;
+        if (packed) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dp, plen, cudaMemcpyDeviceToHost, s));
+        else if (outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaStreamSynchronize(s));
+        const uint64_t nc = h[0];
         outs->n_clamp = nc;
-        outs->edit_count = ec;
-        if (packed) {  // the reference's pack_nbits on the GPU: n * nbits / 8 bytes cross the host link
-            uint8_t *dp = ws.at<uint8_t>(o_pack);
-            if ((rc = pack_deltas_impl(dd, n, nbits, dp, s))) return rc;
-            PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dp, plen, cudaMemcpyDeviceToHost, s));
-        } else if (outs->deltas) {
-            PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
-        }
+        outs->edit_count = h[1];
         if (outs->clamp && nc) PMSZ_CUDA(cudaMemcpyAsync(outs->clamp, dclamp, nc * sizeof(T), cudaMemcpyDeviceToHost, s));
     }
     if (want_verify && (rc = verify_impl<T>(df, dfh, nx, ny, nz, eb, outs->verify, s))) return rc;
