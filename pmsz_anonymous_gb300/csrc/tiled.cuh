@@ -421,20 +421,20 @@ __global__ void __launch_bounds__(kThreads, MODE == kFirst && DEFER && sizeof(T)
 }
 
 // ---------------------------------------------------------------------------
-// TMA-fed first pass.  A block whose tile, halo and planes zb-1 .. ze lie
-// inside the domain gets its planes by tensor-map copies: one thread issues,
-// per plane, a cp.async.bulk.tensor box of f and one of fhat (the tile with
-// its one-voxel halo, widened in x so that the box starts on a 16-byte
-// boundary) into a ring of kRawStages shared-memory stages, each guarded by an
-// mbarrier that the copy engine completes with the box's byte count.  The
-// threads wait for a plane, convert each of its cells to a proxy once (the
-// same conversion and NaN / sentinel check as the load path of tiled_body),
-// and the stage is refilled with the plane kRawStages ahead after the barrier
-// that ends the plane.  No thread computes a global address or predicates a
-// load for the tile; the compute is tiled_body's interior deferring path,
-// except that each voxel stores its own fhat proxy (coalesced) and that the
-// rules of voxels whose codes differ run after the last plane (kRuleCap).
-// Blocks on the domain's faces run tiled_body.
+// TMA-fed first pass.  Every block gets its planes by tensor-map copies: one
+// thread issues, per plane, a cp.async.bulk.tensor box of f and one of fhat
+// (the tile with its one-voxel halo, widened in x so that the box starts on a
+// 16-byte boundary) into a ring of kRawStages shared-memory stages, each
+// guarded by an mbarrier that the copy engine completes with the box's byte
+// count.  The threads wait for a plane, convert each of its cells to a proxy
+// once (the same conversion and NaN / sentinel check as the load path of
+// tiled_body), and the stage is refilled with the plane kRawStages ahead after
+// the barrier that ends the plane.  No thread computes a global address or
+// predicates a load for the tile; the compute is tiled_body's interior
+// deferring path, except that each voxel stores its own fhat proxy
+// (coalesced) and that the rules of voxels whose codes differ run after the
+// last plane (kRuleCap).  Blocks on the domain's faces take the FACE form of
+// the body (first_tma_body).
 //
 // Every mbarrier wait is bounded: a plane that does not arrive within the
 // limit sets *err (the host reports PMSZ_ERR_CUDA), and the block still waits,
