@@ -462,7 +462,7 @@ struct __align__(128) TmaTile {
     alignas(128) unsigned char raw[kRawStages][2][kRawPitch<T>];  // boxes of f and fhat, rows of RawBox<T>::kX
     uint32_t p[2][4][kHY][kHX];                      // proxy ring, as tiled_body's
     uint32_t x[kFirstXCap];                          // voxels whose certificate failed
-    uint32_t rq[kRuleCap];                           // voxels whose codes differ, for the rules (RuleEntry)
+    uint32_t rq[kRuleCap];                           // voxels whose codes differ, queued for the rules
     unsigned long long mbar[kRawStages];
     uint32_t xn, xbase, rn;
 };
