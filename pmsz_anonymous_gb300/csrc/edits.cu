@@ -69,9 +69,11 @@ __device__ __forceinline__ bool fp_lt(T a, T b) {
 
 // cnt (optional): the correction's edit counters; a voxel whose counter is 0
 // was never edited, so cur == prev there and its three values need not be read.
-// Each warp first lists the voxels of its 256 whose value changed (in shared
-// memory), then decides them 32 at a time, so the fp64 work of the decision
-// runs on full warps, about once per 256 voxels instead of once per 32.  Per
+// The block first lists the voxels of its tile whose value changed (in shared
+// memory, voxel order), then decides them 256 at a time, so the fp64 work of
+// the decision runs on full warps (GB300's fp64 pipe issues a warp's
+// instruction at the same cost whether 32 lanes or 4 are active; listed per
+// warp, a few percent of changed voxels filled about a third of the lanes).  Per
 // tile: the clamp flags (one word per 32 voxels, set in shared memory), the
 // clamp count and the edit count, combined in shared memory (no global
 // atomics: one counter shared by every warp serialises at L2).
@@ -87,7 +89,8 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
                                                  uint32_t *__restrict__ tile_edits, int nbits, size_t packed_len) {
     __shared__ uint32_t s_cnt, s_edits;
     __shared__ uint32_t s_fl[kTile / 32];
-    __shared__ uint16_t s_list[8][kTile / 8];  // per warp: changed voxels, offsets within the tile
+    __shared__ uint16_t s_list[kTile];  // the tile's changed voxels (offsets), in voxel order
+    __shared__ uint32_t s_wtot[8];
     __shared__ __align__(8) uint8_t s_sym[PACK ? kTile : 8];  // PACK: the tile's symbols
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_cnt = s_edits = 0;
@@ -135,15 +138,22 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
         const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
         if (lane >= o) inc += t;
     }
-    const uint32_t nt = __shfl_sync(0xFFFFFFFFu, inc, 31);  // warp-uniform
-    uint32_t pos = inc - cnt8;
-    for (uint32_t m = needm; m; m &= m - 1) s_list[w][pos++] = static_cast<uint16_t>(off0 + (__ffs(m) - 1));
-    __syncwarp();
+    if (lane == 31) s_wtot[w] = inc;
+    __syncthreads();
+    uint32_t pos = inc - cnt8, nt = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t u = s_wtot[k];
+        if (k < w) pos += u;
+        nt += u;
+    }
+    for (uint32_t m = needm; m; m &= m - 1) s_list[pos++] = static_cast<uint16_t>(off0 + (__ffs(m) - 1));
+    __syncthreads();
     uint32_t clamps = 0, edits = 0;
-    for (uint32_t k0 = 0; k0 < nt; k0 += 32) {
-        const uint32_t k = k0 + static_cast<uint32_t>(lane);
+    for (uint32_t k0 = 0; k0 < nt; k0 += 256) {  // full warps: the tile's changed voxels, 256 at a time
+        const uint32_t k = k0 + static_cast<uint32_t>(threadIdx.x);
         if (k < nt) {
-            const uint32_t off = s_list[w][k];
+            const uint32_t off = s_list[k];
             const size_t i = base + off;
             const T c = cur[i], p = prev[i];
             edits += fp_lt(c, p);
@@ -162,8 +172,8 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
             else deltas[i] = d;
         }
     }
-    if (PACK) {  // this thread's 8 symbols (all written by its own warp) -> nbits bytes
-        __syncwarp();
+    if (PACK) {  // this thread's 8 symbols -> nbits bytes
+        __syncthreads();
         if (i0 < n) {
             const uint2 u = *reinterpret_cast<const uint2 *>(s_sym + off0);
             const uint64_t mask = (1ull << nbits) - 1ull;
