@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
                                                  const T *__restrict__ f, const uint8_t *__restrict__ cnt, size_t n,
                                                  T eps, T delta, T inv, T quarter, int q, uint8_t *__restrict__ deltas,
                                                  uint32_t *__restrict__ flags, uint32_t *__restrict__ tile_count,
-                                                 uint32_t *__restrict__ tile_edits, int nbits, size_t packed_len) {
+                                                 uint32_t *__restrict__ tile_edits, int nbits, size_t packed_len,
+                                                 uint32_t tile0) {
     __shared__ uint32_t s_cnt, s_edits;
     __shared__ uint32_t s_fl[kTile / 32];
     __shared__ uint16_t s_list[kTile];  // the tile's changed voxels (offsets), in voxel order
@@ -96,7 +97,8 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
     if (threadIdx.x == 0) s_cnt = s_edits = 0;
     if (threadIdx.x < kTile / 32) s_fl[threadIdx.x] = 0;
     __syncthreads();
-    const size_t base = static_cast<size_t>(blockIdx.x) * kTile;
+    const uint32_t tile = tile0 + blockIdx.x;
+    const size_t base = static_cast<size_t>(tile) * kTile;
     // each thread: 8 consecutive voxels (one 8-byte counter load, one 8-byte
     // delta store); the values of the touched ones are loaded together
     const uint32_t off0 = static_cast<uint32_t>(threadIdx.x) * 8;
@@ -197,8 +199,8 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
     if (threadIdx.x < kTile / 32 && base + static_cast<size_t>(threadIdx.x) * 32 < n)
         flags[(base >> 5) + threadIdx.x] = s_fl[threadIdx.x];
     if (threadIdx.x == 0) {
-        tile_count[blockIdx.x] = s_cnt;
-        tile_edits[blockIdx.x] = s_edits;
+        tile_count[tile] = s_cnt;
+        tile_edits[tile] = s_edits;
     }
 }
 
@@ -348,11 +350,15 @@ static void launch_tile_scan(Workspace &ws, const TileScan &t, uint32_t *counts,
 // Enqueues the extraction on s; the clamp and edit totals land in host[0]
 // and host[1] (pinned) once the stream reaches that point.  packed (or
 // null): the symbols packed at nbits bits each instead of one byte per voxel
-// in deltas.  The scratch is released stream-ordered before return.
+// in deltas; with packed_host as well, the tiles are extracted in four
+// ranges and each range's packed symbols are copied to packed_host on a
+// second stream while the next range is extracted (s waits for the copies).
+// The scratch is released stream-ordered before return.
+constexpr int kExtractRanges = 4;
 template <typename T>
 int extract_enqueue(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas,
                     uint8_t *packed, int nbits, T *clamp, unsigned long long *host, cudaStream_t s,
-                    const uint8_t *cnt) {
+                    const uint8_t *cnt, uint8_t *packed_host) {
     if (!prev || !cur || !f || !(deltas || packed) || !clamp || !host) return set_error(PMSZ_ERR_ARG, "null pointer");
     if (n == 0 || n >= (static_cast<size_t>(1) << 32)) return set_error(PMSZ_ERR_ARG, "n must be in 1..2^32-1");
     if (q < 1 || q > 255) return set_error(PMSZ_ERR_ARG, "q must be in 1..255");
@@ -371,18 +377,46 @@ int extract_enqueue(const T *prev, const T *cur, const T *f, size_t n, double eb
     const T eps = static_cast<T>(eb);
     const T delta = static_cast<T>(eb / static_cast<double>(q));
     const T inv = static_cast<T>(1.0 / static_cast<double>(delta)), quarter = static_cast<T>(0.25 * static_cast<double>(delta));
-    if (packed)
+    const size_t plen = (n * static_cast<size_t>(nbits) + 7) / 8;
+    struct Copies {  // released once their work completes
+        cudaStream_t cs = nullptr;
+        cudaEvent_t ev[kExtractRanges + 1] = {};
+        ~Copies() {
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } cp;
+    if (packed && packed_host) {
+        PMSZ_CUDA(cudaStreamCreateWithFlags(&cp.cs, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : cp.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (int r = 0; r < kExtractRanges; ++r) {
+            const size_t t0 = tiles * r / kExtractRanges, t1 = tiles * (r + 1) / kExtractRanges;
+            if (t1 > t0)
+                k_extract<T, true><<<static_cast<unsigned>(t1 - t0), 256, 0, s>>>(
+                    prev, cur, f, cnt, n, eps, delta, inv, quarter, q, packed, flags, tc, te, nbits, plen,
+                    static_cast<uint32_t>(t0));
+            PMSZ_CUDA(cudaEventRecord(cp.ev[r], s));
+            PMSZ_CUDA(cudaStreamWaitEvent(cp.cs, cp.ev[r], 0));
+            const size_t b0 = std::min(plen, t0 * kTile / 8 * static_cast<size_t>(nbits));
+            const size_t b1 = std::min(plen, t1 * kTile / 8 * static_cast<size_t>(nbits));
+            if (b1 > b0)
+                PMSZ_CUDA(cudaMemcpyAsync(packed_host + b0, packed + b0, b1 - b0, cudaMemcpyDeviceToHost, cp.cs));
+        }
+        PMSZ_CUDA(cudaEventRecord(cp.ev[kExtractRanges], cp.cs));
+    } else if (packed) {
         k_extract<T, true><<<static_cast<unsigned>(tiles), 256, 0, s>>>(
-            prev, cur, f, cnt, n, eps, delta, inv, quarter, q, packed, flags, tc, te, nbits,
-            (n * static_cast<size_t>(nbits) + 7) / 8);
-    else
+            prev, cur, f, cnt, n, eps, delta, inv, quarter, q, packed, flags, tc, te, nbits, plen, 0u);
+    } else {
         k_extract<T, false><<<static_cast<unsigned>(tiles), 256, 0, s>>>(prev, cur, f, cnt, n, eps, delta, inv,
-                                                                         quarter, q, deltas, flags, tc, te, 8, 0);
+                                                                         quarter, q, deltas, flags, tc, te, 8, 0, 0u);
+    }
     launch_tile_scan(ws, ts, tc, te, tiles, tot, s);
     k_scatter_clamps<T><<<static_cast<unsigned>((tiles + 7) / 8), 256, 0, s>>>(cur, flags, tc, ws.at<uint32_t>(ts.o_part),
                                                                               n, tiles, clamp);
     PMSZ_CUDA(cudaGetLastError());
     PMSZ_CUDA(cudaMemcpyAsync(host, tot, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if (cp.cs) PMSZ_CUDA(cudaStreamWaitEvent(s, cp.ev[kExtractRanges], 0));  // the symbols' copies, too
     return ws.release();
 }
 
@@ -392,7 +426,7 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
     if (!deltas || !n_clamp || !edit_count) return set_error(PMSZ_ERR_ARG, "null pointer");
     unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
     if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
-    int rc = extract_enqueue<T>(prev, cur, f, n, eb, q, deltas, nullptr, 8, clamp, h, s, cnt);
+    int rc = extract_enqueue<T>(prev, cur, f, n, eb, q, deltas, nullptr, 8, clamp, h, s, cnt, nullptr);
     if (rc) return rc;
     PMSZ_CUDA(cudaStreamSynchronize(s));
     *n_clamp = h[0];
@@ -586,9 +620,11 @@ int reconstruct_impl(const T *prev, const uint8_t *deltas, const T *clamp, uint6
 }
 
 template int extract_enqueue<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *,
-                                    uint8_t *, int, float *, unsigned long long *, cudaStream_t, const uint8_t *);
+                                    uint8_t *, int, float *, unsigned long long *, cudaStream_t, const uint8_t *,
+                                    uint8_t *);
 template int extract_enqueue<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,
-                                     uint8_t *, int, double *, unsigned long long *, cudaStream_t, const uint8_t *);
+                                     uint8_t *, int, double *, unsigned long long *, cudaStream_t, const uint8_t *,
+                                     uint8_t *);
 template int extract_impl<float>(const float *, const float *, const float *, size_t, double, int, uint8_t *, float *,
                                  uint64_t *, uint64_t *, cudaStream_t, const uint8_t *);
 template int extract_impl<double>(const double *, const double *, const double *, size_t, double, int, uint8_t *,

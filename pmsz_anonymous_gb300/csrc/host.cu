@@ -57,10 +57,10 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
         unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
         if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
         uint8_t *dp = packed ? ws.at<uint8_t>(o_pack) : nullptr;
-        if ((rc = extract_enqueue<T>(dprev, dfh, df, n, eb, q, dd, dp, nbits, dclamp, h, s, counted ? dcnt : nullptr)))
+        if ((rc = extract_enqueue<T>(dprev, dfh, df, n, eb, q, dd, dp, nbits, dclamp, h, s, counted ? dcnt : nullptr,
+                                     packed ? static_cast<uint8_t *>(outs->deltas) : nullptr)))
             return rc;
-        if (packed) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dp, plen, cudaMemcpyDeviceToHost, s));
-        else if (outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        if (!packed && outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
         PMSZ_CUDA(cudaStreamSynchronize(s));
         const uint64_t nc = h[0];
         outs->n_clamp = nc;

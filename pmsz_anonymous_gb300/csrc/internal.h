@@ -153,10 +153,12 @@ int extract_impl(const T *prev, const T *cur, const T *f, size_t n, double eb, i
                  uint64_t *n_clamp, uint64_t *edit_count, cudaStream_t s, const uint8_t *cnt = nullptr);
 // The same without the synchronisation: the clamp and edit totals land in
 // host[0], host[1] (pinned) once the stream reaches them; with packed set the
-// symbols go there at nbits bits each (pack_nbits' layout) instead of deltas.
+// symbols go there at nbits bits each (pack_nbits' layout) instead of deltas,
+// and with packed_host as well they are also copied there, range by range,
+// overlapping the extraction (complete when s reaches the end).
 template <typename T>
 int extract_enqueue(const T *prev, const T *cur, const T *f, size_t n, double eb, int q, uint8_t *deltas,
                     uint8_t *packed, int nbits, T *clamp, unsigned long long *host, cudaStream_t s,
-                    const uint8_t *cnt);
+                    const uint8_t *cnt, uint8_t *packed_host);
 
 }  // namespace pmsz
