@@ -114,17 +114,26 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
 #pragma unroll
         for (int j = 0; j < 8; ++j) cv[j] = (i0 + j < n) ? (cnt ? cnt[i0 + j] : uint8_t(1)) : uint8_t(0);
     }
-    T c8[8], p8[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        c8[j] = cv[j] ? cur[i0 + j] : T(0);
-        p8[j] = cv[j] ? prev[i0 + j] : T(0);
-    }
+    // with counters, every counted voxel is listed and the decision below
+    // compares its two values (loaded there anyway); without, the values of
+    // every voxel are compared here
     uint32_t needm = 0;
+    if (cnt) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-        if (cv[j] && !fp_eq(c8[j], p8[j])) needm |= 1u << j;
-    if (PACK) {  // unchanged voxels: symbol 0 (the warp's changed ones are written below)
+        for (int j = 0; j < 8; ++j)
+            if (cv[j]) needm |= 1u << j;
+    } else {
+        T c8[8], p8[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            c8[j] = cv[j] ? cur[i0 + j] : T(0);
+            p8[j] = cv[j] ? prev[i0 + j] : T(0);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (cv[j] && !fp_eq(c8[j], p8[j])) needm |= 1u << j;
+    }
+    if (PACK) {  // voxels not listed: symbol 0 (the listed ones are written below)
         *reinterpret_cast<uint2 *>(s_sym + off0) = make_uint2(0u, 0u);
     } else if (full) {  // unchanged voxels: delta 0; changed ones are written below
         if (needm != 0xFFu) *reinterpret_cast<uint2 *>(deltas + i0) = make_uint2(0u, 0u);
@@ -161,7 +170,9 @@ __global__ void __launch_bounds__(256) k_extract(const T *__restrict__ prev, con
             edits += fp_lt(c, p);
             const T cv = f[i] - eps;
             uint8_t d;
-            if (!fp_eq(c, cv)) {
+            if (fp_eq(c, p)) {  // counted but unchanged (only listed when counters are given)
+                d = 0;
+            } else if (!fp_eq(c, cv)) {
                 d = edit_steps(p, c, delta, inv, quarter, cnt ? static_cast<int>(cnt[i]) : -1);
             } else {
                 d = static_cast<uint8_t>(q);
