@@ -325,70 +325,6 @@ int check_geom(size_t nx, size_t ny, size_t nz) {
     return PMSZ_OK;
 }
 
-// The fused first pass over a field that is still being copied in from the
-// host: slabs of whole z-chunks (about 64 MiB of f + fhat each) go up on a
-// copy stream, each followed by an event; the first pass of a slab's chunks
-// waits for the next slab's event (its tiles read one plane beyond the slab).
-template <typename T>
-int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
-                      uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches,
-                      uint32_t *xlist, uint32_t *xcount, const FirstMaps *maps = nullptr, uint32_t *err = nullptr) {
-    if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
-    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
-    const int nchunks = (g.nz + g.zc - 1) / g.zc;
-    const size_t chunk_bytes = 2 * plane * static_cast<size_t>(g.zc) * sizeof(T);
-    const int cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
-    const int nslabs = (nchunks + cps - 1) / cps;
-    // cs: host copies; ds: device copies of fhat into dprev (kept off cs so
-    // the host link never idles behind them)
-    struct Res {
-        cudaStream_t cs = nullptr, ds = nullptr;
-        std::vector<cudaEvent_t> ev;
-        cudaEvent_t done = nullptr;
-        ~Res() {  // released once pending work completes
-            for (cudaEvent_t e : ev)
-                if (e) cudaEventDestroy(e);
-            if (done) cudaEventDestroy(done);
-            if (cs) cudaStreamDestroy(cs);
-            if (ds) cudaStreamDestroy(ds);
-        }
-    } r;
-    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
-    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.ds, cudaStreamNonBlocking));
-    r.ev.assign(static_cast<size_t>(nslabs) + 1, nullptr);
-    for (cudaEvent_t &e : r.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    PMSZ_CUDA(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
-    PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
-    PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
-    for (int j = 0; j < nslabs; ++j) {
-        const size_t z0 = static_cast<size_t>(j) * cps * g.zc;
-        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * g.zc);
-        const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
-        PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
-        PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
-        PMSZ_CUDA(cudaEventRecord(r.ev[j], r.cs));
-        if (in.dprev) {
-            PMSZ_CUDA(cudaStreamWaitEvent(r.ds, r.ev[j], 0));
-            PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.ds));
-        }
-    }
-    PMSZ_CUDA(cudaEventRecord(r.done, in.dprev ? r.ds : r.cs));
-    const dim3 blk3(kTX, kTY, 1);
-    for (int j = 0; j < nslabs; ++j) {
-        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
-        dim3 grid = tiled_grid(g);
-        grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
-        if (xlist)  // deferring first pass (see k_first_exact)
-            launch_first_pass<T>(*maps, grid, s, f, fh, codes, hp, req, a_next, slot, g, j * cps, xlist, xcount, err);
-        else
-            k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
-        PMSZ_CUDA(cudaGetLastError());
-        ++*launches;
-    }
-    PMSZ_CUDA(cudaStreamWaitEvent(s, r.done, 0));  // dprev complete before the first edit
-    return PMSZ_OK;
-}
-
 // Slabs of the host-buffer copy: whole z-chunks, about 64 MiB of f + fhat.
 struct IngestSlabs {
     int cps, nchunks, nslabs;
@@ -401,6 +337,74 @@ static IngestSlabs ingest_slabs(const Geom &g, size_t elem) {
     r.cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
     r.nslabs = (r.nchunks + r.cps - 1) / r.cps;
     return r;
+}
+
+template <typename T>
+int enqueue_ingest(const T *hf, const T *hfh, T *df, T *dfh, T *dprev, size_t nx, size_t ny, size_t nz,
+                   cudaStream_t s, IngestCopies &c) {
+    int rc = check_geom(nx, ny, nz);
+    if (rc) return rc;
+    Geom g = make_geom(nx, ny, nz);
+    g.zc = tuned_zchunk(nx, ny, nz, sizeof(T));  // the tile depth correct_impl will use
+    const IngestSlabs sl = ingest_slabs(g, sizeof(T));
+    c.cps = sl.cps;
+    c.nchunks = sl.nchunks;
+    c.nslabs = sl.nslabs;
+    c.zc = g.zc;
+    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
+    // cs: host copies; ds: device copies of fhat into dprev (kept off cs so
+    // the host link never idles behind them)
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&c.cs, cudaStreamNonBlocking));
+    PMSZ_CUDA(cudaStreamCreateWithFlags(&c.ds, cudaStreamNonBlocking));
+    c.ev.assign(static_cast<size_t>(c.nslabs) + 1, nullptr);
+    c.evp.assign(static_cast<size_t>(c.nslabs), nullptr);
+    for (cudaEvent_t &e : c.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaEvent_t &e : c.evp) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PMSZ_CUDA(cudaEventRecord(c.ev[c.nslabs], s));  // the destinations are allocated
+    PMSZ_CUDA(cudaStreamWaitEvent(c.cs, c.ev[c.nslabs], 0));
+    for (int j = 0; j < c.nslabs; ++j) {
+        const size_t z0 = static_cast<size_t>(j) * c.cps * g.zc;
+        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * c.cps * g.zc);
+        const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
+        PMSZ_CUDA(cudaMemcpyAsync(df + off, hf + off, bytes, cudaMemcpyHostToDevice, c.cs));
+        PMSZ_CUDA(cudaMemcpyAsync(dfh + off, hfh + off, bytes, cudaMemcpyHostToDevice, c.cs));
+        PMSZ_CUDA(cudaEventRecord(c.ev[j], c.cs));
+        if (dprev) {  // the pre-correction copy of fhat, before any edit of the slab
+            PMSZ_CUDA(cudaStreamWaitEvent(c.ds, c.ev[j], 0));
+            PMSZ_CUDA(cudaMemcpyAsync(dprev + off, dfh + off, bytes, cudaMemcpyDeviceToDevice, c.ds));
+            PMSZ_CUDA(cudaEventRecord(c.evp[j], c.ds));
+        } else {
+            PMSZ_CUDA(cudaEventRecord(c.evp[j], c.cs));
+        }
+    }
+    return PMSZ_OK;
+}
+
+// The fused first pass over a field that is still being copied in from the
+// host (the copies of enqueue_ingest): the first pass of a slab's chunks waits
+// for the next slab's event (its tiles read one plane beyond the slab).
+template <typename T>
+int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
+                      uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches,
+                      uint32_t *xlist, uint32_t *xcount, const FirstMaps *maps = nullptr, uint32_t *err = nullptr) {
+    if (in.df != f || !in.copies || in.copies->zc != g.zc)
+        return set_error(PMSZ_ERR_ARG, "ingest copies do not match the field");
+    const IngestCopies &r = *in.copies;
+    const int cps = r.cps, nchunks = r.nchunks, nslabs = r.nslabs;
+    const dim3 blk3(kTX, kTY, 1);
+    for (int j = 0; j < nslabs; ++j) {
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
+        dim3 grid = tiled_grid(g);
+        grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
+        if (xlist)  // deferring first pass (see k_first_exact)
+            launch_first_pass<T>(*maps, grid, s, f, fh, codes, hp, req, a_next, slot, g, j * cps, xlist, xcount, err);
+        else
+            k_tiled<T, kFirst><<<grid, blk3, 0, s>>>(f, fh, codes, hp, req, a_next, slot, g, j * cps);
+        PMSZ_CUDA(cudaGetLastError());
+        ++*launches;
+    }
+    PMSZ_CUDA(cudaStreamWaitEvent(s, r.evp[nslabs - 1], 0));  // dprev complete before the first edit
+    return PMSZ_OK;
 }
 
 // Sweeps pipelined behind the host copy (even: the graph's two-sweep body
@@ -446,46 +450,11 @@ static int first_pass_waves(const HostIngest<T> &in, const T *f, T *fh, uint8_t 
                             uint32_t *req, uint32_t *const act[2], SweepSlot *slots, LoopState *ls, const Geom &g,
                             const FirstMaps &maps, uint32_t *list, uint32_t *xlist, uint32_t *slist, uint32_t *bcnt,
                             const FastDiv &div_nx, T eps, T delta, int q, int K, cudaStream_t s, int64_t *launches) {
-    if (in.df != f) return set_error(PMSZ_ERR_ARG, "ingest destination differs from the field");
-    const size_t plane = static_cast<size_t>(g.nx) * g.ny;
-    const IngestSlabs sl = ingest_slabs(g, sizeof(T));
-    const int cps = sl.cps, nchunks = sl.nchunks, nslabs = sl.nslabs;
+    if (in.df != f || !in.copies || in.copies->zc != g.zc)
+        return set_error(PMSZ_ERR_ARG, "ingest copies do not match the field");
+    const IngestCopies &r = *in.copies;
+    const int cps = r.cps, nchunks = r.nchunks, nslabs = r.nslabs;
     const unsigned lb = 152 * 8;
-    struct Res {
-        cudaStream_t cs = nullptr, ds = nullptr;
-        std::vector<cudaEvent_t> ev, evp;
-        ~Res() {  // released once pending work completes
-            for (cudaEvent_t e : ev)
-                if (e) cudaEventDestroy(e);
-            for (cudaEvent_t e : evp)
-                if (e) cudaEventDestroy(e);
-            if (cs) cudaStreamDestroy(cs);
-            if (ds) cudaStreamDestroy(ds);
-        }
-    } r;
-    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
-    PMSZ_CUDA(cudaStreamCreateWithFlags(&r.ds, cudaStreamNonBlocking));
-    r.ev.assign(static_cast<size_t>(nslabs) + 1, nullptr);
-    r.evp.assign(static_cast<size_t>(nslabs), nullptr);
-    for (cudaEvent_t &e : r.ev) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    for (cudaEvent_t &e : r.evp) PMSZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    PMSZ_CUDA(cudaEventRecord(r.ev[nslabs], s));  // scratch and destinations are ready
-    PMSZ_CUDA(cudaStreamWaitEvent(r.cs, r.ev[nslabs], 0));
-    for (int j = 0; j < nslabs; ++j) {
-        const size_t z0 = static_cast<size_t>(j) * cps * g.zc;
-        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * cps * g.zc);
-        const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
-        PMSZ_CUDA(cudaMemcpyAsync(in.df + off, in.hf + off, bytes, cudaMemcpyHostToDevice, r.cs));
-        PMSZ_CUDA(cudaMemcpyAsync(fh + off, in.hfh + off, bytes, cudaMemcpyHostToDevice, r.cs));
-        PMSZ_CUDA(cudaEventRecord(r.ev[j], r.cs));
-        if (in.dprev) {  // the pre-correction copy of fhat, before any edit of the slab
-            PMSZ_CUDA(cudaStreamWaitEvent(r.ds, r.ev[j], 0));
-            PMSZ_CUDA(cudaMemcpyAsync(in.dprev + off, fh + off, bytes, cudaMemcpyDeviceToDevice, r.ds));
-            PMSZ_CUDA(cudaEventRecord(r.evp[j], r.ds));
-        } else {
-            PMSZ_CUDA(cudaEventRecord(r.evp[j], r.cs));
-        }
-    }
     std::vector<int> Dp(static_cast<size_t>(K) + 1, 0), Ap(static_cast<size_t>(K) + 1, 0);  // fronts so far
     std::vector<char> wave_after(static_cast<size_t>(nslabs), 0);
     auto mark = [&](int e) { wave_after[static_cast<size_t>(std::max(1, (nslabs * e + 15) / 16) - 1)] = 1; };
@@ -537,6 +506,11 @@ static int first_pass_waves(const HostIngest<T> &in, const T *f, T *fh, uint8_t 
     return PMSZ_OK;
 }
 
+template int enqueue_ingest<float>(const float *, const float *, float *, float *, float *, size_t, size_t, size_t,
+                                   cudaStream_t, IngestCopies &);
+template int enqueue_ingest<double>(const double *, const double *, double *, double *, double *, size_t, size_t,
+                                    size_t, cudaStream_t, IngestCopies &);
+
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
                  pmsz_result *res, cudaStream_t s, const HostIngest<T> *ingest) {
@@ -576,7 +550,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     // (first_pass_waves; K even, below max_sweeps); their detection spills go
     // to a list of their own (xlist still collects the first pass's deferrals)
     const int wave_k = static_cast<int>(std::min<int64_t>(kWaveSweeps, max_sweeps - 1)) & ~1;
-    const bool waves = ingest && use_list && wave_k >= 2 && ingest_slabs(g, sizeof(T)).nslabs >= 2;
+    const bool waves = ingest && use_list && wave_k >= 2 && ingest->copies && ingest->copies->nslabs >= 2;
     const size_t o_slist = ws.reserve<uint32_t>(waves ? g.n : 0);
     if ((rc = ws.commit())) return rc;
     uint32_t *hp = ws.at<uint32_t>(o_hp);

@@ -43,8 +43,11 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
         if (want_edits) PMSZ_CUDA(cudaMemcpyAsync(dprev, dfh, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
         st = naive_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s);
     } else {
-        // the copies in overlap the fused first pass (slab by slab)
-        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr, dcnt};
+        // the copies in start now and overlap the fused first pass (slab by
+        // slab) and the sweeps behind it
+        IngestCopies copies;
+        if ((rc = enqueue_ingest<T>(f, fhat, df, dfh, want_edits ? dprev : nullptr, nx, ny, nz, s, copies))) return rc;
+        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr, dcnt, &copies};
         st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s, &in);
     }
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;

@@ -99,11 +99,41 @@ int check_geom(size_t nx, size_t ny, size_t nz);
 // fh); dprev, if not null, receives a device copy of the input fhat; cnt, if
 // not null, is a caller buffer of n bytes the correction uses as its edit
 // counters (left holding them for the edit extraction).
+// The slab copies of a host-buffer call (enqueue_ingest): slab j's f and
+// fhat go up on cs, then ev[j]; the pre-correction copy of slab j's fhat
+// into dprev follows on ds, then evp[j] (without dprev, evp[j] marks ev[j]'s
+// point).  Slabs are whole z-chunks of the tile depth, about 64 MiB of f +
+// fhat each (cps chunks).  Events and streams are released once their work
+// completes.
+struct IngestCopies {
+    cudaStream_t cs = nullptr, ds = nullptr;
+    std::vector<cudaEvent_t> ev, evp;
+    int cps = 0, nchunks = 0, nslabs = 0, zc = 0;
+    IngestCopies() = default;
+    IngestCopies(const IngestCopies &) = delete;
+    IngestCopies &operator=(const IngestCopies &) = delete;
+    ~IngestCopies() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : evp)
+            if (e) cudaEventDestroy(e);
+        if (cs) cudaStreamDestroy(cs);
+        if (ds) cudaStreamDestroy(ds);
+    }
+};
+// Enqueues the copies of a host-buffer call as soon as the destinations df,
+// dfh (and dprev) exist on s: the copy stream waits for s only up to here,
+// not for the correction's own setup.
+template <typename T>
+int enqueue_ingest(const T *hf, const T *hfh, T *df, T *dfh, T *dprev, size_t nx, size_t ny, size_t nz,
+                   cudaStream_t s, IngestCopies &c);
+
 template <typename T>
 struct HostIngest {
     const T *hf, *hfh;
     T *df, *dprev;
     uint8_t *cnt;
+    const IngestCopies *copies;  // enqueued by enqueue_ingest
 };
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,
