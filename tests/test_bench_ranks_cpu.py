@@ -35,7 +35,7 @@ def _rank(rank, world, port, out):
 
 def test_two_ranks_take_the_max_time_and_count_all_voxels():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork: the pytest process may hold a CUDA context
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
