@@ -326,6 +326,11 @@ int check_geom(size_t nx, size_t ny, size_t nz) {
 }
 
 // Slabs of the host-buffer copy: whole z-chunks, about 64 MiB of f + fhat.
+// The copy of slab j ends one plane past its chunks (planes b_j .. b_{j+1} - 1
+// with b_j = j * cps * zc + 1, b_0 = 0, the last ending at nz), so the first
+// pass of slab j's chunks, whose tiles read one plane beyond them, waits for
+// the copy of slab j only: once the host link delivers the last slab, one
+// slab's first pass is left, not two.
 struct IngestSlabs {
     int cps, nchunks, nslabs;
 };
@@ -337,6 +342,11 @@ static IngestSlabs ingest_slabs(const Geom &g, size_t elem) {
     r.cps = static_cast<int>(std::max<size_t>(1, (static_cast<size_t>(64) << 20) / chunk_bytes));
     r.nslabs = (r.nchunks + r.cps - 1) / r.cps;
     return r;
+}
+static size_t slab_begin(int j, int cps, int nslabs, int zc, size_t nz) {
+    if (j <= 0) return 0;
+    if (j >= nslabs) return nz;
+    return std::min(nz, static_cast<size_t>(j) * cps * zc + 1);  // j * cps * zc < nz for j < nslabs
 }
 
 template <typename T>
@@ -363,15 +373,18 @@ int enqueue_ingest(const T *hf, const T *hfh, T *df, T *dfh, T *dprev, size_t nx
     PMSZ_CUDA(cudaEventRecord(c.ev[c.nslabs], s));  // the destinations are allocated
     PMSZ_CUDA(cudaStreamWaitEvent(c.cs, c.ev[c.nslabs], 0));
     for (int j = 0; j < c.nslabs; ++j) {
-        const size_t z0 = static_cast<size_t>(j) * c.cps * g.zc;
-        const size_t z1 = std::min<size_t>(g.nz, static_cast<size_t>(j + 1) * c.cps * g.zc);
+        const size_t z0 = slab_begin(j, c.cps, c.nslabs, g.zc, g.nz);
+        const size_t z1 = slab_begin(j + 1, c.cps, c.nslabs, g.zc, g.nz);
         const size_t off = z0 * plane, bytes = (z1 - z0) * plane * sizeof(T);
-        PMSZ_CUDA(cudaMemcpyAsync(df + off, hf + off, bytes, cudaMemcpyHostToDevice, c.cs));
-        PMSZ_CUDA(cudaMemcpyAsync(dfh + off, hfh + off, bytes, cudaMemcpyHostToDevice, c.cs));
+        if (bytes) {
+            PMSZ_CUDA(cudaMemcpyAsync(df + off, hf + off, bytes, cudaMemcpyHostToDevice, c.cs));
+            PMSZ_CUDA(cudaMemcpyAsync(dfh + off, hfh + off, bytes, cudaMemcpyHostToDevice, c.cs));
+        }
         PMSZ_CUDA(cudaEventRecord(c.ev[j], c.cs));
         if (dprev) {  // the pre-correction copy of fhat, before any edit of the slab
             PMSZ_CUDA(cudaStreamWaitEvent(c.ds, c.ev[j], 0));
-            PMSZ_CUDA(cudaMemcpyAsync(dprev + off, dfh + off, bytes, cudaMemcpyDeviceToDevice, c.ds));
+            if (bytes)
+                PMSZ_CUDA(cudaMemcpyAsync(dprev + off, dfh + off, bytes, cudaMemcpyDeviceToDevice, c.ds));
             PMSZ_CUDA(cudaEventRecord(c.evp[j], c.ds));
         } else {
             PMSZ_CUDA(cudaEventRecord(c.evp[j], c.cs));
@@ -382,7 +395,7 @@ int enqueue_ingest(const T *hf, const T *hfh, T *df, T *dfh, T *dprev, size_t nx
 
 // The fused first pass over a field that is still being copied in from the
 // host (the copies of enqueue_ingest): the first pass of a slab's chunks waits
-// for the next slab's event (its tiles read one plane beyond the slab).
+// for that slab's event (its copy includes the plane beyond the chunks).
 template <typename T>
 int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes, uint32_t *hp, uint32_t *req,
                       uint32_t *a_next, SweepSlot *slot, const Geom &g, cudaStream_t s, int64_t *launches,
@@ -393,7 +406,7 @@ int first_pass_ingest(const HostIngest<T> &in, const T *f, T *fh, uint8_t *codes
     const int cps = r.cps, nchunks = r.nchunks, nslabs = r.nslabs;
     const dim3 blk3(kTX, kTY, 1);
     for (int j = 0; j < nslabs; ++j) {
-        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[j], 0));
         dim3 grid = tiled_grid(g);
         grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
         if (xlist)  // deferring first pass (see k_first_exact)
@@ -429,7 +442,7 @@ static __global__ void k_wave_clear_spills(LoopState *ls) {
     if (threadIdx.x == 0 && blockIdx.x == 0) ls->lc[2] = 0;
 }
 
-// The host-buffer wavefront.  The copy of slab j + 1 releases the first pass
+// The host-buffer wavefront.  The copy of slab j releases the first pass
 // of slab j (sweep 0's detection, complete below plane Z = (j + 1) * slab
 // depth, or nz after the last slab); after the slabs of kWaveAt8 / kWaveAt4
 // follows a wave: on the planes already final, the pieces of sweeps 0 .. K that those
@@ -464,7 +477,7 @@ static int first_pass_waves(const HostIngest<T> &in, const T *f, T *fh, uint8_t 
         for (int e : kWaveAt4) mark(e);
     for (int j = 0; j < nslabs; ++j) {
         const bool last = j == nslabs - 1;
-        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[std::min(j + 1, nslabs - 1)], 0));
+        PMSZ_CUDA(cudaStreamWaitEvent(s, r.ev[j], 0));
         dim3 grid = tiled_grid(g);
         grid.z = static_cast<unsigned>(std::min(cps, nchunks - j * cps));
         launch_first_pass<T>(maps, grid, s, f, fh, codes, hp, req, act[1], &slots[0], g, j * cps, xlist, &ls->lc[3],
@@ -678,8 +691,9 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
                 ++bodies;
             }
         } else {
-            // The graph: one conditional while node whose body is enqueue_body,
-            // captured while sweep 0 runs; no host round trip between sweeps.
+            // The graph: k_loop_enter, then one conditional while node whose
+            // body is enqueue_body, captured while sweep 0 runs; no host round
+            // trip between sweeps.
             struct GraphGuard {
                 cudaGraph_t graph = nullptr;
                 cudaGraphExec_t exec = nullptr;
@@ -698,8 +712,18 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             cp.conditional.handle = cond;
             cp.conditional.type = cudaGraphCondTypeWhile;
             cp.conditional.size = 1;
-            cudaGraphNode_t wnode;
-            PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, nullptr, nullptr, 0, &cp));
+            // k_loop_enter sets the condition before the while node is reached
+            const LoopState *cls = ls;
+            void *eargs[] = {&cls, &cond};
+            cudaGraphNodeParams ep = {};
+            ep.type = cudaGraphNodeTypeKernel;
+            ep.kernel.func = reinterpret_cast<void *>(k_loop_enter);
+            ep.kernel.gridDim = dim3(1);
+            ep.kernel.blockDim = dim3(32);
+            ep.kernel.kernelParams = eargs;
+            cudaGraphNode_t enode, wnode;
+            PMSZ_CUDA(cudaGraphAddNode(&enode, gg.graph, nullptr, nullptr, 0, &ep));
+            PMSZ_CUDA(cudaGraphAddNode(&wnode, gg.graph, &enode, nullptr, 1, &cp));
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             PMSZ_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
             PMSZ_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
@@ -710,15 +734,24 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[3], s));
 
-        LoopState *hls = static_cast<LoopState *>(host_pinned(sizeof(LoopState)));
-        if (!hls) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+        // the loop state and the first slots of the sweep log in one round trip
+        constexpr int64_t kLogAhead = 64;
+        const int64_t pre = std::min<int64_t>(max_sweeps, kLogAhead);
+        const size_t ls_bytes = (sizeof(LoopState) + 63) / 64 * 64;
+        unsigned char *hb = static_cast<unsigned char *>(host_pinned(ls_bytes + static_cast<size_t>(pre) * sizeof(SweepSlot)));
+        if (!hb) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+        LoopState *hls = reinterpret_cast<LoopState *>(hb);
+        const SweepSlot *hlog = reinterpret_cast<const SweepSlot *>(hb + ls_bytes);
         PMSZ_CUDA(cudaMemcpyAsync(hls, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
+        PMSZ_CUDA(cudaMemcpyAsync(hb + ls_bytes, slots, static_cast<size_t>(pre) * sizeof(SweepSlot),
+                                  cudaMemcpyDeviceToHost, s));
         PMSZ_CUDA(cudaStreamSynchronize(s));
         if (hls->err)
             return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
         const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
         const int64_t nloop = std::max<int64_t>(done - (waves ? wave_k + 1 : 1), 0);  // sweeps of the loop
-        launches += 16 * ((flags & PMSZ_FLAG_HOST_LOOP) ? bodies : std::max<int64_t>(1, (nloop + 1) / 2));
+        // graph: k_loop_enter and one body (16 kernels) per two sweeps that ran
+        launches += (flags & PMSZ_FLAG_HOST_LOOP) ? 16 * bodies : 1 + 16 * ((nloop + 1) / 2);
         if (timing) {  // the list sweeps' edits run inside the graph and count as detection time
             float a = 0, b = 0, c = 0;
             PMSZ_CUDA(cudaEventElapsedTime(&a, lt.ev[0], lt.ev[1]));
@@ -728,10 +761,13 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             ms_apply += b;
             ms_detect += c;
         }
-        log.resize(static_cast<size_t>(done));
-        PMSZ_CUDA(cudaMemcpyAsync(log.data(), slots, static_cast<size_t>(done) * sizeof(SweepSlot),
-                                  cudaMemcpyDeviceToHost, s));
-        PMSZ_CUDA(cudaStreamSynchronize(s));
+        log.assign(hlog, hlog + std::min(done, pre));
+        if (done > pre) {
+            log.resize(static_cast<size_t>(done));
+            PMSZ_CUDA(cudaMemcpyAsync(log.data() + pre, slots + pre, static_cast<size_t>(done - pre) * sizeof(SweepSlot),
+                                      cudaMemcpyDeviceToHost, s));
+            PMSZ_CUDA(cudaStreamSynchronize(s));
+        }
         for (const SweepSlot &t : log) edits += t.requested;
         sweeps = done;
         const SweepSlot h = log.back();

@@ -536,6 +536,12 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
     if (set_cond) cudaGraphSetConditional(cond, ls->go ? 1u : 0u);
 }
 
+// The graph node ahead of the while node: the loop's first body runs only if
+// the gate before the graph let the next sweep run.
+static __global__ void k_loop_enter(const LoopState *ls, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(cond, ls->go ? 1u : 0u);
+}
+
 // After the host-buffer wavefront has run sweeps 0 .. K to the end: the loop
 // state that k_loop_gate would have left after sweep K, or after the first of
 // those sweeps that stops the loop (the sweeps after a stopping one changed
