@@ -309,6 +309,47 @@ static int run_sweep_loop(const T *f, T *fh, const uint8_t *codes, uint8_t *cnt,
     return ws.release();
 }
 
+// The cooperative tail behind the list sweeps, enqueued without waiting for
+// the host: it starts at sweep ls->k and runs only if the last gate handed
+// over to it (ls->tail); *hdone (pinned host memory) receives the total
+// number of sweeps once the stream gets there.
+template <typename T>
+static int enqueue_gated_tail(const T *f, T *fh, const uint8_t *codes, uint8_t *cnt, uint32_t *hp, uint32_t *req,
+                              uint32_t *const act[2], SweepSlot *slots, const LoopState *ls, int64_t max_sweeps,
+                              const Geom &g, T eps, T delta, int q, cudaStream_t s, EventTimer *et, long long *hdone) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    PMSZ_CUDA(cudaGetDevice(&dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return set_error(PMSZ_ERR_CUDA, "device does not support cooperative launches");
+    PMSZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tail_loop<T>, kTailBlock, 0));
+    if (per_sm < 1) return set_error(PMSZ_ERR_CUDA, "sweep loop kernel does not fit on an SM");
+    const size_t ns = summary_words(g);
+    const unsigned grid = static_cast<unsigned>(std::max<size_t>(1, std::min<size_t>(ns, static_cast<size_t>(per_sm) * sms)));
+    Workspace ws(s);
+    const size_t o_done = ws.reserve<long long>(1);
+    const size_t o_sum = ws.reserve<uint32_t>(3 * ns);
+    int rc = ws.commit();
+    if (rc) return rc;
+    long long *d_done = ws.at<long long>(o_done);
+    uint32_t *sum = ws.at<uint32_t>(o_sum);  // summaries of act[0], act[1], req
+    if (et) PMSZ_CUDA(cudaEventRecord(et->ev[0], s));
+    PMSZ_CUDA(cudaMemsetAsync(sum, 0, 3 * ns * sizeof(uint32_t), s));
+    k_build_summary_at<<<static_cast<unsigned>(std::min<size_t>((ns + 7) / 8, 152 * 16)), 256, 0, s>>>(
+        act[0], act[1], g, sum, sum + ns, &ls->k, &ls->tail);
+    PMSZ_CUDA(cudaGetLastError());
+    TailArgs<T> a{f,    fh,        codes, cnt, hp,    req, act[0], act[1], sum + 2 * ns, sum, sum + ns,
+                  slots, 0, max_sweeps, d_done, g,  eps, delta,  q};
+    a.first_at = &ls->k;
+    a.run_if = &ls->tail;
+    void *args[] = {&a};
+    PMSZ_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k_tail_loop<T>), dim3(grid), dim3(kTailBlock),
+                                          args, 0, s));
+    if (et) PMSZ_CUDA(cudaEventRecord(et->ev[1], s));
+    PMSZ_CUDA(cudaMemcpyAsync(hdone, d_done, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    return ws.release();
+}
+
 // Grid of the list-compaction kernels: one block per 2048-word round, at most
 // 16 blocks per SM (grid-stride beyond).
 static inline unsigned list_grid(const Geom &g) {
@@ -604,6 +645,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
     int64_t sweeps = 0;
     uint64_t edits = 0;
     int status = PMSZ_ERR_NOT_CONVERGED;
+    bool end_recorded = false;  // et.ev[0] marks the end of the correction's device window
     std::vector<SweepSlot> log;
     // The cooperative tail takes over once the next active set is estimated
     // below N/32, but never above kTailCap voxels: its barrier-separated
@@ -734,22 +776,40 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         if (timing) PMSZ_CUDA(cudaEventRecord(lt.ev[3], s));
 
-        // the loop state and the first slots of the sweep log in one round trip
+        // The cooperative tail follows without a host round trip (it reads
+        // the gate's decision), then the caller's work on the result; one
+        // read-back brings the loop state, the sweep count and the first
+        // slots of the sweep log.
         constexpr int64_t kLogAhead = 64;
         const int64_t pre = std::min<int64_t>(max_sweeps, kLogAhead);
         const size_t ls_bytes = (sizeof(LoopState) + 63) / 64 * 64;
-        unsigned char *hb = static_cast<unsigned char *>(host_pinned(ls_bytes + static_cast<size_t>(pre) * sizeof(SweepSlot)));
+        unsigned char *hb =
+            static_cast<unsigned char *>(host_pinned(ls_bytes + 64 + static_cast<size_t>(pre) * sizeof(SweepSlot)));
         if (!hb) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
         LoopState *hls = reinterpret_cast<LoopState *>(hb);
-        const SweepSlot *hlog = reinterpret_cast<const SweepSlot *>(hb + ls_bytes);
+        long long *hdone = reinterpret_cast<long long *>(hb + ls_bytes);
+        const SweepSlot *hlog = reinterpret_cast<const SweepSlot *>(hb + ls_bytes + 64);
+        EventTimer tt;
+        if (timing && (rc = tt.init())) return rc;
+        if ((rc = enqueue_gated_tail<T>(f, fh, codes, cnt, hp, req, act, slots, ls, max_sweeps, g, eps, delta, q, s,
+                                        timing ? &tt : nullptr, hdone)))
+            return rc;
+        launches += 2;
+        PMSZ_CUDA(cudaEventRecord(et.ev[0], s));  // end of the correction's device window
+        end_recorded = true;
         PMSZ_CUDA(cudaMemcpyAsync(hls, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
-        PMSZ_CUDA(cudaMemcpyAsync(hb + ls_bytes, slots, static_cast<size_t>(pre) * sizeof(SweepSlot),
+        PMSZ_CUDA(cudaMemcpyAsync(hb + ls_bytes + 64, slots, static_cast<size_t>(pre) * sizeof(SweepSlot),
                                   cudaMemcpyDeviceToHost, s));
+        if (ingest && ingest->after && ingest->after->fn) {
+            ingest->after->done = true;
+            if ((rc = ingest->after->fn(s))) return rc;
+        }
         PMSZ_CUDA(cudaStreamSynchronize(s));
         if (hls->err)
             return set_error(PMSZ_ERR_CUDA, "first pass: a tile plane's tensor copy did not arrive within the bounded wait");
-        const int64_t done = hls->k;  // sweeps 0 .. done-1 ran
-        const int64_t nloop = std::max<int64_t>(done - (waves ? wave_k + 1 : 1), 0);  // sweeps of the loop
+        const int64_t gdone = hls->k;  // sweeps 0 .. gdone-1 ran before the tail
+        const int64_t done = std::max<int64_t>(*hdone, gdone);  // and 0 .. done-1 in all
+        const int64_t nloop = std::max<int64_t>(gdone - (waves ? wave_k + 1 : 1), 0);  // sweeps of the loop
         // graph: k_loop_enter and one body (16 kernels) per two sweeps that ran
         launches += (flags & PMSZ_FLAG_HOST_LOOP) ? 16 * bodies : 1 + 16 * ((nloop + 1) / 2);
         if (timing) {  // the list sweeps' edits run inside the graph and count as detection time
@@ -760,6 +820,10 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
             ms_first += a;
             ms_apply += b;
             ms_detect += c;
+            if (hls->tail) {
+                PMSZ_CUDA(cudaEventElapsedTime(&a, tt.ev[0], tt.ev[1]));
+                ms_detect += a;
+            }
         }
         log.assign(hlog, hlog + std::min(done, pre));
         if (done > pre) {
@@ -770,34 +834,18 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         for (const SweepSlot &t : log) edits += t.requested;
         sweeps = done;
-        const SweepSlot h = log.back();
-        if (sweeps == 1 && h.bad) {
+        const SweepSlot h = log[static_cast<size_t>(gdone - 1)];  // the sweep the last gate judged
+        if (gdone == 1 && h.bad) {
             status = set_error(PMSZ_ERR_ARG, "input contains NaN or the value 1e30 (the reference's halo sentinel)");
         } else if (h.fmax == 0 && h.fmin == 0 && h.fdir == 0) {
             status = PMSZ_OK;
         } else if (h.progressed == 0) {
             set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
-        } else if (sweeps < max_sweeps) {  // the gate handed the rest to the cooperative tail
-            int64_t done2 = 0;
-            if ((rc = run_sweep_loop<T>(f, fh, codes, cnt, hp, req, act, slots, sweeps, max_sweeps, g, eps, delta, q,
-                                        s, timing ? &et : nullptr, &ms_detect, &done2)))
-                return rc;
-            ++launches;
-            const size_t m = static_cast<size_t>(done2 - sweeps);
-            if (m) {
-                std::vector<SweepSlot> tail(m);
-                PMSZ_CUDA(cudaMemcpyAsync(tail.data(), slots + sweeps, m * sizeof(SweepSlot), cudaMemcpyDeviceToHost, s));
-                PMSZ_CUDA(cudaStreamSynchronize(s));
-                for (const SweepSlot &t : tail) {
-                    log.push_back(t);
-                    edits += t.requested;
-                }
-                const SweepSlot &last = tail.back();
-                if (last.fmax == 0 && last.fmin == 0 && last.fdir == 0) status = PMSZ_OK;
-                else if (last.progressed == 0)
-                    set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
-            }
-            sweeps = done2;
+        } else if (done > gdone) {  // the cooperative tail ran sweeps gdone .. done-1
+            const SweepSlot &last = log.back();
+            if (last.fmax == 0 && last.fmin == 0 && last.fdir == 0) status = PMSZ_OK;
+            else if (last.progressed == 0)
+                set_error(PMSZ_ERR_NOT_CONVERGED, "a sweep requested edits that changed nothing (all requested vertices clamped)");
         }
     }
     while (!use_list && sweeps < max_sweeps) {
@@ -874,7 +922,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
     }
     float ms_total = 0;
-    PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
+    if (!end_recorded) PMSZ_CUDA(cudaEventRecord(et.ev[0], s));
     PMSZ_CUDA(cudaEventSynchronize(et.ev[0]));
     PMSZ_CUDA(cudaEventElapsedTime(&ms_total, et.ev[3], et.ev[0]));
     if (status == PMSZ_ERR_NOT_CONVERGED && sweeps >= max_sweeps)

@@ -36,6 +36,26 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
     T *df = ws.at<T>(o_f), *dfh = ws.at<T>(o_fh), *dprev = ws.at<T>(o_prev), *dclamp = ws.at<T>(o_c);
     uint8_t *dd = ws.at<uint8_t>(o_d);
     uint8_t *dcnt = want_edits ? ws.at<uint8_t>(o_cnt) : nullptr;
+    // the edit output: enqueued by the correction right behind its last
+    // kernel where it can (no host round trip in between), else below.  The
+    // symbols (packed on the GPU at nbits bits, the reference's pack_nbits,
+    // when asked: n * nbits / 8 bytes cross the host link) go back during the
+    // extraction; the clamp and edit totals land in h.
+    const bool counted = !(opts && (opts->flags & PMSZ_FLAG_NAIVE));  // the pMSz loop leaves its counters in dcnt
+    unsigned long long *h = nullptr;
+    AfterCorrection after;
+    if (want_edits) {
+        h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long), 1));
+        if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+        uint8_t *dp = packed ? ws.at<uint8_t>(o_pack) : nullptr;
+        after.fn = [=](cudaStream_t st) -> int {
+            int r = extract_enqueue<T>(dprev, dfh, df, n, eb, q, dd, dp, nbits, dclamp, h, st, counted ? dcnt : nullptr,
+                                       packed ? static_cast<uint8_t *>(outs->deltas) : nullptr);
+            if (r) return r;
+            if (!packed && outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, st));
+            return PMSZ_OK;
+        };
+    }
     int st;
     if (opts && (opts->flags & PMSZ_FLAG_NAIVE)) {
         PMSZ_CUDA(cudaMemcpyAsync(df, f, n * sizeof(T), cudaMemcpyHostToDevice, s));
@@ -47,23 +67,13 @@ int host_impl(const T *f, T *fhat, size_t nx, size_t ny, size_t nz, double eb, c
         // slab) and the sweeps behind it
         IngestCopies copies;
         if ((rc = enqueue_ingest<T>(f, fhat, df, dfh, want_edits ? dprev : nullptr, nx, ny, nz, s, copies))) return rc;
-        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr, dcnt, &copies};
+        const HostIngest<T> in{f, fhat, df, want_edits ? dprev : nullptr, dcnt, &copies, want_edits ? &after : nullptr};
         st = correct_impl<T>(df, dfh, nx, ny, nz, eb, opts, res, s, &in);
     }
     if (st != PMSZ_OK && st != PMSZ_ERR_NOT_CONVERGED) return st;
     std::string keep = st == PMSZ_ERR_NOT_CONVERGED ? pmsz_last_error() : std::string();
     if (want_edits) {
-        // the symbols (packed on the GPU at nbits bits, the reference's
-        // pack_nbits, when asked: n * nbits / 8 bytes cross the host link) go
-        // back while the host waits for the clamp count
-        const bool counted = !(opts && (opts->flags & PMSZ_FLAG_NAIVE));  // the pMSz loop left its counters in dcnt
-        unsigned long long *h = static_cast<unsigned long long *>(host_pinned(2 * sizeof(unsigned long long)));
-        if (!h) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
-        uint8_t *dp = packed ? ws.at<uint8_t>(o_pack) : nullptr;
-        if ((rc = extract_enqueue<T>(dprev, dfh, df, n, eb, q, dd, dp, nbits, dclamp, h, s, counted ? dcnt : nullptr,
-                                     packed ? static_cast<uint8_t *>(outs->deltas) : nullptr)))
-            return rc;
-        if (!packed && outs->deltas) PMSZ_CUDA(cudaMemcpyAsync(outs->deltas, dd, n, cudaMemcpyDeviceToHost, s));
+        if (!after.done && (rc = after.fn(s))) return rc;
         PMSZ_CUDA(cudaStreamSynchronize(s));
         const uint64_t nc = h[0];
         outs->n_clamp = nc;

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <new>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/pmsz.h"
@@ -86,8 +87,9 @@ struct EventTimer {
     }
 };
 
-// Pinned host memory for per-sweep counter read-back, one block per thread.
-void *host_pinned(size_t bytes);
+// Pinned host memory for per-sweep counter read-back: per thread, one block
+// per slot (0: the correction's read-back, 1: the edit output's totals).
+void *host_pinned(size_t bytes, int slot = 0);
 
 // Implementations behind the C entry points (explicitly instantiated for
 // float and double in their translation units).
@@ -128,12 +130,21 @@ template <typename T>
 int enqueue_ingest(const T *hf, const T *hfh, T *df, T *dfh, T *dprev, size_t nx, size_t ny, size_t nz,
                    cudaStream_t s, IngestCopies &c);
 
+// Work the caller wants on the stream right behind the correction's last
+// kernel and ahead of its read-back (the host-buffer edit output): fn is
+// called once, by correct_impl where its path allows (done is then set),
+// else by the caller after it.
+struct AfterCorrection {
+    std::function<int(cudaStream_t)> fn;
+    bool done = false;
+};
 template <typename T>
 struct HostIngest {
     const T *hf, *hfh;
     T *df, *dprev;
     uint8_t *cnt;
     const IngestCopies *copies;  // enqueued by enqueue_ingest
+    AfterCorrection *after;      // or null
 };
 template <typename T>
 int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, const pmsz_opts *opts,

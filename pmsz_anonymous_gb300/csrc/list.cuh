@@ -485,6 +485,7 @@ inline void compact_bitmap_planes(uint32_t *bm, const Geom &g, int z0, int z1, u
 struct LoopState {
     long long k;
     int go;
+    int tail;        // the loop stopped only because the next active set is small: the cooperative tail runs
     int exact_keys;  // fp32 list detection on exact keys (k_pick_detection)
     uint32_t lc[4];  // active list, request list, exact list (spills), first-pass deferrals
     uint32_t deferred;  // voxels of the current list sweep decided on exact keys
@@ -528,6 +529,7 @@ static __global__ void k_loop_gate(LoopState *ls, SweepSlot *slots, long long ma
                           k + 1 >= max_sweeps;
         const bool tail = 15ull * c.changed + c.fdir <= tail_at;
         ls->go = (!stop && !tail) ? 1 : 0;
+        ls->tail = (!stop && tail) ? 1 : 0;
         ls->k = k + 1;
         ls->cur = SweepSlot{};
         ls->lc[0] = ls->lc[1] = ls->lc[2] = ls->lc[3] = 0;
@@ -562,10 +564,12 @@ static __global__ void k_wave_gate(LoopState *ls, const SweepSlot *slots, long l
     if (stop) {
         ls->k = k + 1;
         ls->go = 0;
+        ls->tail = 0;
     } else {
         const SweepSlot c = slots[K];
         ls->k = K + 1;
         ls->go = 15ull * c.changed + c.fdir <= tail_at ? 0 : 1;
+        ls->tail = 1 - ls->go;
     }
     const unsigned long long deferred = ls->lc[3];
     const unsigned long long est = 15ull * slots[0].changed + slots[0].fdir;

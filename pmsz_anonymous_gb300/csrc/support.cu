@@ -51,12 +51,13 @@ int Workspace::release() {
     return PMSZ_OK;
 }
 
-void *host_pinned(size_t bytes) {
+void *host_pinned(size_t bytes, int slot) {
     struct Block {
         void *p = nullptr;
         size_t n = 0;
     };
-    static thread_local Block b;  // lives until process exit
+    static thread_local Block blocks[2];  // live until process exit
+    Block &b = blocks[slot == 1 ? 1 : 0];
     if (b.n < bytes) {
         void *p = nullptr;
         if (cudaMallocHost(&p, bytes) != cudaSuccess) {

@@ -64,8 +64,7 @@ __device__ __forceinline__ void request_targets_s(uint32_t *req, uint32_t *sum, 
 
 // Summary of a plain bitmap (at the hand-over to the tail): one warp per
 // summary word, lane j testing word j of its 32.
-static __global__ void __launch_bounds__(256) k_build_summary(const uint32_t *__restrict__ bm, Geom g,
-                                                       uint32_t *__restrict__ sum) {
+__device__ __forceinline__ void build_summary(const uint32_t *__restrict__ bm, const Geom &g, uint32_t *__restrict__ sum) {
     const size_t ns = summary_words(g);
     const int lane = threadIdx.x & 31;
     const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x >> 5);
@@ -74,6 +73,19 @@ static __global__ void __launch_bounds__(256) k_build_summary(const uint32_t *__
         const uint32_t bits = __ballot_sync(0xFFFFFFFFu, w < g.nwords && bm[w] != 0);
         if (lane == 0) sum[s] = bits;
     }
+}
+static __global__ void __launch_bounds__(256) k_build_summary(const uint32_t *__restrict__ bm, Geom g,
+                                                       uint32_t *__restrict__ sum) {
+    build_summary(bm, g, sum);
+}
+// The same for a tail launched ahead of the host's decision: nothing unless
+// *run_if, and the bitmap of sweep *k_at (act0 / sum0 for even sweeps).
+static __global__ void __launch_bounds__(256) k_build_summary_at(const uint32_t *act0, const uint32_t *act1, Geom g,
+                                                          uint32_t *sum0, uint32_t *sum1, const long long *k_at,
+                                                          const int *run_if) {
+    if (!*run_if) return;
+    const bool odd = (*k_at & 1) != 0;
+    build_summary(odd ? act1 : act0, g, odd ? sum1 : sum0);
 }
 
 constexpr uint32_t kTailListCap = 4096;
@@ -294,6 +306,10 @@ struct TailArgs {
     Geom g;
     T eps, delta;
     int q;
+    // launched ahead of the host's decision (run_if not null): the first
+    // sweep is *first_at, and nothing runs unless *run_if
+    const long long *first_at = nullptr;
+    const int *run_if = nullptr;
 };
 
 // Sweep k reads (act[k & 1], sum[k & 1]) and fills (act[(k + 1) & 1], ...).
@@ -302,6 +318,13 @@ __global__ void __launch_bounds__(kTailBlock, 2) k_tail_loop(TailArgs<T> a) {
     __shared__ TailSmem sm;
     cg::grid_group grid = cg::this_grid();
     int64_t k = a.first;
+    if (a.run_if) {  // every block reads the same flag: all return, or none
+        k = __ldcg(a.first_at);
+        if (!__ldcg(a.run_if)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) *a.sweeps_out = k;
+            return;
+        }
+    }
     while (true) {
         const SweepSlot *p = a.slots + (k - 1);
         if (sweep_stops(__ldcg(&p->fmax), __ldcg(&p->fmin), __ldcg(&p->fdir), __ldcg(&p->progressed), k,
