@@ -418,6 +418,29 @@ int MultiRun<T>::loop(int64_t *iters) {
     return PMSZ_OK;
 }
 
+template <typename T>
+int MultiRun<T>::enqueue_loop(long long *hiters) {
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    PMSZ_CUDA(cudaGetDevice(&dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PMSZ_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return set_error(PMSZ_ERR_CUDA, "device does not support cooperative launches");
+    PMSZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_loop_multi<T>, kListBlock, 0));
+    if (per_sm < 1) return set_error(PMSZ_ERR_CUDA, "loop kernel does not fit on an SM");
+    const unsigned grid = static_cast<unsigned>(
+        std::max<size_t>(1, std::min<size_t>(total_rounds, static_cast<size_t>(per_sm) * sms)));
+    const Inst<T> *a0 = dinst;
+    const uint32_t *a1 = drpre;
+    int a2 = n;
+    uint32_t a3 = total_rounds;
+    long long *a4 = diters;
+    void *args[] = {&a0, &a1, &a2, &a3, &a4};
+    PMSZ_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(k_loop_multi<T>), dim3(grid),
+                                          dim3(kListBlock), args, 0, s));
+    PMSZ_CUDA(cudaMemcpyAsync(hiters, diters, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    return PMSZ_OK;
+}
+
 template struct MultiRun<float>;
 template struct MultiRun<double>;
 
@@ -477,17 +500,17 @@ static int run_gated(MultiRun<T> &run, int64_t max_sweeps, std::vector<BatchOutc
     PMSZ_CUDA(cudaGraphInstantiate(&gg.exec, gg.graph, 0));
     PMSZ_CUDA(cudaGraphLaunch(gg.exec, s));
 
-    BatchState hs;
-    PMSZ_CUDA(cudaMemcpyAsync(&hs, st, sizeof(BatchState), cudaMemcpyDeviceToHost, s));
+    // The rest of the live fields in the cooperative tail, enqueued at once:
+    // it reads the table the last gate left on the device and, with no field
+    // left running, ends at its first iteration.  One read-back follows.
+    unsigned char *hb = static_cast<unsigned char *>(host_pinned(128 + sizeof(BatchState)));
+    if (!hb) return set_error(PMSZ_ERR_OOM, "pinned host allocation failed");
+    long long *hiters = reinterpret_cast<long long *>(hb);
+    BatchState *hs = reinterpret_cast<BatchState *>(hb + 128);
+    if ((rc = run.enqueue_loop(hiters))) return rc;
+    PMSZ_CUDA(cudaMemcpyAsync(hs, st, sizeof(BatchState), cudaMemcpyDeviceToHost, s));
     PMSZ_CUDA(cudaStreamSynchronize(s));
-    int64_t total = hs.k;  // sweeps 0 .. total-1 ran as generations
-    if (hs.live > 0) {     // the rest of the live fields in the cooperative tail
-        PMSZ_CUDA(cudaMemcpyAsync(run.host.data(), run.dinst, n * sizeof(Inst<T>), cudaMemcpyDeviceToHost, s));
-        PMSZ_CUDA(cudaStreamSynchronize(s));
-        int64_t iters = 0;
-        if ((rc = run.loop(&iters))) return rc;
-        total += iters;
-    }
+    const int64_t total = hs->k + *hiters;  // generations 0 .. hs->k - 1, then the tail's iterations
     std::vector<SweepSlot> rows;
     if ((rc = run.read_rows(0, total, rows))) return rc;
     for (int i = 0; i < n; ++i) {

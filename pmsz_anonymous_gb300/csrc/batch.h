@@ -80,6 +80,9 @@ struct MultiRun {
     int generation();
     // The remaining sweeps of all active fields in one cooperative launch.
     int loop(int64_t *iters);
+    // The same launch on the device table as it stands when the stream gets
+    // there, without waiting: *hiters (pinned) receives the iteration count.
+    int enqueue_loop(long long *hiters);
     int read_row(int64_t k, std::vector<SweepSlot> &row);
     // rows k .. k+count-1 in one copy (row j at out[j * n])
     int read_rows(int64_t k, int64_t count, std::vector<SweepSlot> &out);
