@@ -129,7 +129,7 @@ int parse(int argc, char **argv, Args &a) {
     a.py = std::atoi(pos[k + 3].c_str());
     a.pz = std::atoi(pos[k + 4].c_str());
     if (a.px != 1 || a.py != 1 || a.pz != 1)
-        return usage("this build corrects a field on one GPU per process: PX PY PZ must be 1 1 1");
+        return usage("this program corrects a field on one GPU per process: PX PY PZ must be 1 1 1");
     return 0;
 }
 

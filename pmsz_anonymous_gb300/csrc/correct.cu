@@ -834,7 +834,7 @@ int correct_impl(const T *f, T *fh, size_t nx, size_t ny, size_t nz, double eb, 
         }
         for (const SweepSlot &t : log) edits += t.requested;
         sweeps = done;
-        const SweepSlot h = log[static_cast<size_t>(gdone - 1)];  // the sweep the last gate judged
+        const SweepSlot h = log[static_cast<size_t>(gdone - 1)];  // the sweep the last gate decided on
         if (gdone == 1 && h.bad) {
             status = set_error(PMSZ_ERR_ARG, "input contains NaN or the value 1e30 (the reference's halo sentinel)");
         } else if (h.fmax == 0 && h.fmin == 0 && h.fdir == 0) {
